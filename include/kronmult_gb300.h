@@ -1,0 +1,160 @@
+/*
+ * kronmult_gb300.h -- C ABI of the GB300 (sm_103a) batched Kronecker mat-vec.
+ *
+ *   Y(:,k) += kron(A1(:,:,k), ..., Ad(:,:,k)) * X(:,k),   d = 1..6
+ *
+ * Conventions, identical to hipdac-lab/kronmult:
+ *   - factors are column-major with a leading dimension; A_l(i,j) = A_l[i + j*ld];
+ *   - an X/Y block is a vector whose LAST Kronecker index runs fastest, so
+ *     kron(A1,...,Ad) has A1's index slowest (test_kronmult6_batched.cpp:418-436);
+ *   - Y is accumulated into, never overwritten (kronmultv.hpp:178);
+ *   - every array and every pointer array is DEVICE memory; the pointer arrays
+ *     themselves live on the device (test_kronmult6_xbatched.cpp:318-321);
+ *   - calls are asynchronous on the given stream (0 = legacy default stream);
+ *     the caller synchronises, as with the reference (test_kronmult6_batched.cpp:248).
+ *
+ * Differences from the reference, all supersets of its contract:
+ *   - each call returns a kmx_status instead of asserting;
+ *   - X is never modified (the reference may clobber X in batched/pbatched);
+ *   - W is used only when one entry does not fit on chip; it may then be
+ *     clobbered exactly as in the reference.
+ */
+#ifndef KRONMULT_GB300_H
+#define KRONMULT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without pulling in cuda_runtime.h. */
+typedef struct CUstream_st* kmx_stream_t;
+
+typedef enum kmx_status {
+  KMX_OK = 0,
+  KMX_ERR_INVALID_ARG = 1,   /* d outside 1..6, n < 1, batch < 0, lda < n, ... */
+  KMX_ERR_NULL_POINTER = 2,  /* a required array pointer is NULL */
+  KMX_ERR_WORKSPACE = 3,     /* workspace missing or too small for an entry */
+  KMX_ERR_UNSUPPORTED = 4,   /* shape or option this build does not handle */
+  KMX_ERR_CUDA = 5,          /* a CUDA runtime call failed (see kmx_last_cuda_error) */
+  KMX_ERR_DEVICE = 6,        /* a kernel reported an error through the device status word */
+  KMX_ERR_OVERLAP = 7        /* deterministic mode: Y blocks partially overlap */
+} kmx_status;
+
+/* Arithmetic form of the FP64 entry points. */
+typedef enum kmx_form {
+  KMX_FORM_AUTO = 0,   /* per-(d,n) choice from the tuning table */
+  KMX_FORM_PLAIN = 1,  /* native FP64 fused multiply-add */
+  KMX_FORM_SPLIT = 2   /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
+                          ~2^-47 relative per operation, FP64 in and out */
+} kmx_form;
+
+/* How contributions of entries that share a Y block are combined. */
+typedef enum kmx_accumulate {
+  KMX_ACC_ATOMIC = 0,        /* FP64/FP32 atomic add per element (reference semantics) */
+  KMX_ACC_DETERMINISTIC = 1  /* entries grouped by Y block on the device, each block summed
+                                in a fixed order and written once: bitwise reproducible */
+} kmx_accumulate;
+
+typedef struct kmx_options {
+  int form;        /* kmx_form */
+  int accumulate;  /* kmx_accumulate */
+  int transpose;   /* nonzero: use A_l^T for every factor (the backward dX product) */
+} kmx_options;
+
+/* ---------------------------------------------------------------------- */
+/* Drop-in entry points (FP64), argument order of the reference.           */
+/* ---------------------------------------------------------------------- */
+
+/* kronmult{d}_batched (reference kronmult6_batched.cpp:5-25).
+ * A is (n,n,d,batch); X, Y, W are (n^d, batch), contiguous. */
+int kmx_kronmult_batched_f64(int d, int n, const double* A, double* X, double* Y, double* W,
+                             int batchCount, kmx_stream_t stream);
+
+/* kronmult{d}_pbatched (reference kronmult6_pbatched.cpp:5-25).
+ * A is (n,n,d,batch); pX/pY/pW are arrays of batch device pointers to
+ * n^d-element blocks; Y blocks may alias. */
+int kmx_kronmult_pbatched_f64(int d, int n, const double* A, double* const* pX,
+                              double* const* pY, double* const* pW, int batchCount,
+                              kmx_stream_t stream);
+
+/* kronmult{d}_xbatched (reference kronmult6_xbatched.cpp:5-39).
+ * Aarray is (d, batch) pointers to n x n factors with leading dimension lda
+ * (0 means n); Y blocks may alias.  pW holds 2*subbatchCount workspace
+ * pointers when batchCount > 1 (subbatchCount 0 means max(1, batch/2)) and
+ * one when batchCount == 1, exactly as the reference; it is read only when an
+ * entry does not fit on chip. */
+int kmx_kronmult_xbatched_f64(int d, int n, const double* const* Aarray, int lda,
+                              double* const* pX, double* const* pY, double* const* pW,
+                              int batchCount, int subbatchCount, kmx_stream_t stream);
+
+/* kronmult{d}_vbatched (reference kronmult6_vbatched.hpp:16-29, which has no
+ * host wrapper).  Factor l is m[l] x n[l] with leading dimension m[l],
+ * uniform over the batch; Aarray is (d, batch).  W is one workspace of
+ * Wcapacity_bytes, used only when an entry does not fit on chip. */
+int kmx_kronmult_vbatched_f64(int d, const int* m, const int* n, const double* const* Aarray,
+                              double* const* pX, double* const* pY, double* W,
+                              size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream);
+
+/* FP32 storage forms of the same four entry points (the reference's float
+ * templates).  Arithmetic is FP32 fused multiply-add. */
+int kmx_kronmult_batched_f32(int d, int n, const float* A, float* X, float* Y, float* W,
+                             int batchCount, kmx_stream_t stream);
+int kmx_kronmult_pbatched_f32(int d, int n, const float* A, float* const* pX, float* const* pY,
+                              float* const* pW, int batchCount, kmx_stream_t stream);
+int kmx_kronmult_xbatched_f32(int d, int n, const float* const* Aarray, int lda,
+                              float* const* pX, float* const* pY, float* const* pW,
+                              int batchCount, int subbatchCount, kmx_stream_t stream);
+int kmx_kronmult_vbatched_f32(int d, const int* m, const int* n, const float* const* Aarray,
+                              float* const* pX, float* const* pY, float* W,
+                              size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Extended entry points: same arguments plus options (NULL = defaults).   */
+/* ---------------------------------------------------------------------- */
+int kmx_kronmult_batched_f64_ex(int d, int n, const double* A, double* X, double* Y, double* W,
+                                int batchCount, const kmx_options* opt, kmx_stream_t stream);
+int kmx_kronmult_pbatched_f64_ex(int d, int n, const double* A, double* const* pX,
+                                 double* const* pY, double* const* pW, int batchCount,
+                                 const kmx_options* opt, kmx_stream_t stream);
+int kmx_kronmult_xbatched_f64_ex(int d, int n, const double* const* Aarray, int lda,
+                                 double* const* pX, double* const* pY, double* const* pW,
+                                 int batchCount, int subbatchCount, const kmx_options* opt,
+                                 kmx_stream_t stream);
+int kmx_kronmult_vbatched_f64_ex(int d, const int* m, const int* n,
+                                 const double* const* Aarray, double* const* pX,
+                                 double* const* pY, double* W, size_t Wcapacity_bytes,
+                                 int batchCount, const kmx_options* opt, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Library state and diagnostics.                                          */
+/* ---------------------------------------------------------------------- */
+
+/* Default options used by the drop-in entry points (process-wide). */
+void kmx_set_default_options(const kmx_options* opt);
+void kmx_get_default_options(kmx_options* opt);
+
+/* Reads and clears the current device's status word, written by kernels
+ * that met a NULL pointer inside a pointer array or a wait that ran out.
+ * Synchronises the stream.  Returns KMX_OK or KMX_ERR_DEVICE; *flags gets
+ * the raw bits (may be NULL). */
+int kmx_check_device_status(kmx_stream_t stream, int* flags);
+
+/* The last CUDA error code seen by the library on this thread. */
+int kmx_last_cuda_error(void);
+
+/* Human-readable name of a kmx_status. */
+const char* kmx_status_string(int status);
+
+/* Flops of one entry, 2 * sum over the recursion levels (kroncommon.hpp:204-234). */
+double kmx_kron_flops(int d, const int* m, const int* n);
+
+/* Version string of this build. */
+const char* kmx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KRONMULT_GB300_H */

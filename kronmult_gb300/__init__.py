@@ -1,0 +1,203 @@
+"""kronmult_gb300 -- batched Kronecker mat-vec on GB300 (sm_103a).
+
+    Y(:,k) += kron(A1(:,:,k), ..., Ad(:,:,k)) * X(:,k),   d = 1..6
+
+Python host side of the C ABI in ``include/kronmult_gb300.h``.  Arrays are
+torch CUDA tensors (or raw device addresses); pointer arrays are int64 CUDA
+tensors holding device addresses, as the reference's pointer-array entry
+points expect device-resident ``T*[]`` arrays.
+
+The per-dimension names of the reference (``kronmult6_xbatched`` ...) are
+provided with the reference's argument order (kronmult6_xbatched.cpp:5-13 and
+siblings); ``kronmult_batched`` etc. take d explicitly.  Every call launches
+asynchronously on the current torch stream (or ``stream=``) and raises
+``KmxError`` on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._lib import KmxError, check, exported_symbols, lib, options  # noqa: F401
+
+__all__ = [
+    "KmxError", "lib", "options", "kron_flops", "pointer_array", "check_device_status",
+    "kronmult_batched", "kronmult_pbatched", "kronmult_xbatched", "kronmult_vbatched",
+    "set_default_form",
+]
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _addr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    t = _torch()
+    if not isinstance(x, t.Tensor):
+        raise TypeError(f"expected a CUDA tensor or an address, got {type(x)}")
+    if not x.is_cuda:
+        raise ValueError("arrays must be CUDA tensors (device memory)")
+    return x.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return _torch().cuda.current_stream().cuda_stream
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def _is_f64(dtype) -> bool:
+    t = _torch()
+    if dtype in (t.float64, "f64", "float64"):
+        return True
+    if dtype in (t.float32, "f32", "float32"):
+        return False
+    raise TypeError(f"unsupported dtype {dtype}")
+
+
+def pointer_array(base, offsets, itemsize: int | None = None):
+    """int64 CUDA tensor of device addresses ``base + offsets * itemsize``."""
+    t = _torch()
+    offs = t.as_tensor(offsets, dtype=t.int64, device=base.device)
+    isz = base.element_size() if itemsize is None else itemsize
+    return offs * isz + base.data_ptr()
+
+
+def kron_flops(d, m, n=None) -> float:
+    """Flops of one entry (kroncommon.hpp:204-234)."""
+    if isinstance(m, int):
+        m = [m] * d
+    n = m if n is None else ([n] * d if isinstance(n, int) else n)
+    mm = (C.c_int * d)(*m)
+    nn = (C.c_int * d)(*n)
+    return float(lib().kmx_kron_flops(d, mm, nn))
+
+
+def set_default_form(form: str = "auto", accumulate: str = "atomic") -> None:
+    """Process-wide defaults of the drop-in entry points."""
+    o = options(form, accumulate)
+    lib().kmx_set_default_options(C.byref(o))
+
+
+def check_device_status(stream=None) -> int:
+    """Read and clear the device status word; raises KmxError if set."""
+    flags = C.c_int(0)
+    rc = lib().kmx_check_device_status(C.c_void_p(_stream(stream)), C.byref(flags))
+    check(rc, "kmx_check_device_status")
+    return flags.value
+
+
+def _opt(form, accumulate, transpose):
+    if form is None and accumulate is None and not transpose:
+        return None
+    return C.byref(options(form or "auto", accumulate or "atomic", transpose))
+
+
+def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accumulate=None,
+                     transpose=False, stream=None):
+    """kronmult{d}_batched: A (n,n,d,batch) column-major, X/Y/W (n^d, batch)."""
+    f64 = _is_f64(A.dtype)
+    b = batchCount if batchCount is not None else X.numel() // (n ** d)
+    s = C.c_void_p(_stream(stream))
+    L = lib()
+    if f64:
+        rc = L.kmx_kronmult_batched_f64_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
+                                           _opt(form, accumulate, transpose), s)
+    else:
+        if form not in (None, "auto", "plain") or transpose or accumulate not in (None, "atomic"):
+            raise KmxError(4, "kmx_kronmult_batched_f32")
+        rc = L.kmx_kronmult_batched_f32(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b, s)
+    check(rc, f"kronmult{d}_batched")
+
+
+def kronmult_pbatched(d, n, A, pX, pY, pW=None, batchCount=None, *, form=None, accumulate=None,
+                      transpose=False, stream=None):
+    """kronmult{d}_pbatched: A (n,n,d,batch); pX/pY/pW int64 address tensors."""
+    f64 = _is_f64(A.dtype)
+    b = batchCount if batchCount is not None else pX.numel()
+    s = C.c_void_p(_stream(stream))
+    L = lib()
+    if f64:
+        rc = L.kmx_kronmult_pbatched_f64_ex(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b,
+                                            _opt(form, accumulate, transpose), s)
+    else:
+        rc = L.kmx_kronmult_pbatched_f32(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b, s)
+    check(rc, f"kronmult{d}_pbatched")
+
+
+def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subbatchCount=0, *,
+                      dtype=None, form=None, accumulate=None, transpose=False, stream=None):
+    """kronmult{d}_xbatched: Aarray (d, batch) factor addresses with leading
+    dimension lda; pX/pY/pW address arrays.  dtype is float64 unless given."""
+    t = _torch()
+    f64 = _is_f64(dtype if dtype is not None else t.float64)
+    b = batchCount if batchCount is not None else pX.numel()
+    s = C.c_void_p(_stream(stream))
+    L = lib()
+    if f64:
+        rc = L.kmx_kronmult_xbatched_f64_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
+                                            _addr(pW), b, subbatchCount,
+                                            _opt(form, accumulate, transpose), s)
+    else:
+        rc = L.kmx_kronmult_xbatched_f32(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
+                                         _addr(pW), b, subbatchCount, s)
+    check(rc, f"kronmult{d}_xbatched")
+
+
+def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, batchCount=None, *,
+                      dtype=None, form=None, accumulate=None, transpose=False, stream=None):
+    """kronmult{d}_vbatched: factor l is m[l] x n[l] (ld = m[l]) for every entry."""
+    t = _torch()
+    f64 = _is_f64(dtype if dtype is not None else t.float64)
+    b = batchCount if batchCount is not None else pX.numel()
+    mm = (C.c_int * d)(*[int(v) for v in m])
+    nn = (C.c_int * d)(*[int(v) for v in n])
+    cap = Wcapacity_bytes if Wcapacity_bytes is not None else (
+        W.numel() * W.element_size() if W is not None else 0)
+    s = C.c_void_p(_stream(stream))
+    L = lib()
+    if f64:
+        rc = L.kmx_kronmult_vbatched_f64_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
+                                            _addr(W), cap, b, _opt(form, accumulate, transpose), s)
+    else:
+        rc = L.kmx_kronmult_vbatched_f32(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY), _addr(W),
+                                         cap, b, s)
+    check(rc, f"kronmult{d}_vbatched")
+
+
+# Reference names, one per d, reference argument order.
+def _make(d):
+    def batched(n, Aarray_, Xarray_, Yarray_, Warray_, batchCount, **kw):
+        kronmult_batched(d, n, Aarray_, Xarray_, Yarray_, Warray_, batchCount, **kw)
+
+    def pbatched(n, Aarray_, pX_, pY_, pW_, batchCount, **kw):
+        kronmult_pbatched(d, n, Aarray_, pX_, pY_, pW_, batchCount, **kw)
+
+    def xbatched(n, Aarray_, lda, pX_, pY_, pW_, batchCount, subbatchCount=0, **kw):
+        kronmult_xbatched(d, n, Aarray_, lda, pX_, pY_, pW_, batchCount, subbatchCount, **kw)
+
+    def vbatched(*args, **kw):
+        mn = args[: 2 * d]
+        rest = args[2 * d:]
+        m = list(mn[0::2])
+        n = list(mn[1::2])
+        Aarray_, pX_, pY_, W_, Wcap, batchCount = rest
+        kronmult_vbatched(d, m, n, Aarray_, pX_, pY_, W_, Wcap, batchCount, **kw)
+
+    return batched, pbatched, xbatched, vbatched
+
+
+for _d in range(1, 7):
+    _b, _p, _x, _v = _make(_d)
+    for _kind, _fn in (("batched", _b), ("pbatched", _p), ("xbatched", _x), ("vbatched", _v)):
+        _fn.__name__ = f"kronmult{_d}_{_kind}"
+        globals()[_fn.__name__] = _fn
+        __all__.append(_fn.__name__)
+del _d, _b, _p, _x, _v, _kind, _fn

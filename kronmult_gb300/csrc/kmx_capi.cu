@@ -1,0 +1,433 @@
+// kmx_capi.cu -- the C ABI (include/kronmult_gb300.h): argument validation,
+// problem set-up and dispatch to the per-form launchers.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+#include "../../include/kronmult_gb300.h"
+#include "kmx_forms.h"
+#include "kmx_launch.cuh"
+
+namespace kmx {
+
+// Device status word written by kernels (NULL pointer met inside a pointer
+// array, a bounded wait that ran out).  Read and cleared by
+// kmx_check_device_status.
+__device__ int g_status_word;
+
+namespace {
+
+constexpr int MAX_DEVICES = 64;
+thread_local int t_last_cuda_error = 0;
+
+std::mutex g_mu;
+DeviceInfo g_dev[MAX_DEVICES];
+bool g_dev_ok[MAX_DEVICES];
+int* g_status_ptr[MAX_DEVICES];
+std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
+
+kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0};
+bool g_default_init = false;
+
+void init_defaults_locked() {
+  if (g_default_init) return;
+  g_default_init = true;
+  const char* f = std::getenv("KMX_FORM");
+  if (f) {
+    if (!std::strcmp(f, "plain")) g_default.form = KMX_FORM_PLAIN;
+    else if (!std::strcmp(f, "split")) g_default.form = KMX_FORM_SPLIT;
+    else if (!std::strcmp(f, "auto")) g_default.form = KMX_FORM_AUTO;
+  }
+}
+
+kmx_options resolve_options(const kmx_options* opt) {
+  if (opt) return *opt;
+  std::lock_guard<std::mutex> lk(g_mu);
+  init_defaults_locked();
+  return g_default;
+}
+
+int cuda_fail(cudaError_t e) {
+  t_last_cuda_error = (int)e;
+  return KMX_ERR_CUDA;
+}
+
+int status_ptr(int** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e);
+  if (dev < 0 || dev >= MAX_DEVICES) return KMX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_status_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_status_word);
+    if (e != cudaSuccess) return cuda_fail(e);
+    g_status_ptr[dev] = static_cast<int*>(p);
+  }
+  *out = g_status_ptr[dev];
+  return KMX_OK;
+}
+
+bool ipow_checked(int n, int d, long long* out) {
+  long long r = 1;
+  for (int i = 0; i < d; ++i) {
+    r *= n;
+    if (r > (1LL << 31) - 1) return false;
+  }
+  *out = r;
+  return true;
+}
+
+}  // namespace
+
+DeviceInfo device_info(int dev) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (dev >= 0 && dev < MAX_DEVICES && g_dev_ok[dev]) return g_dev[dev];
+  DeviceInfo di;
+  cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&di.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&di.max_threads_per_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  if (dev >= 0 && dev < MAX_DEVICES) {
+    g_dev[dev] = di;
+    g_dev_ok[dev] = true;
+  }
+  return di;
+}
+
+cudaError_t ensure_smem(const void* func, int dev, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto& m = g_smem_set[dev];
+  auto it = m.find(func);
+  if (it != m.end() && it->second >= bytes) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) m[func] = bytes;
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// Common driver: validated Problem -> launcher of the requested form.
+// ---------------------------------------------------------------------------
+static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream_t s) {
+  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  int rc = status_ptr(&p.status);
+  if (rc != KMX_OK) return rc;
+  LaunchHint h = {0, 0, 0};
+  cudaError_t e;
+  if (!is_f64) {
+    e = launch_f32_plain(p, h, s);
+  } else {
+    int form = o.form;
+    if (form == KMX_FORM_AUTO) {
+      const bool spec = is_square(p) && (p.n[0] >= 2 && p.n[0] <= 8 || p.n[0] == 16);
+      form = spec ? KMX_FORM_SPLIT : KMX_FORM_PLAIN;
+    }
+    if (form == KMX_FORM_SPLIT) {
+      e = launch_f64_split(p, h, s);
+      if (e == cudaErrorNotSupported) e = launch_f64_plain(p, h, s);
+    } else if (form == KMX_FORM_PLAIN) {
+      e = launch_f64_plain(p, h, s);
+    } else {
+      return KMX_ERR_INVALID_ARG;
+    }
+  }
+  if (e == cudaErrorInvalidValue) return KMX_ERR_WORKSPACE;
+  if (e == cudaErrorNotSupported) return KMX_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e);
+  return KMX_OK;
+}
+
+static void base_square(Problem& p, int layout, int d, int n, int ld, long long N) {
+  std::memset(&p, 0, sizeof(p));
+  p.layout = layout;
+  p.d = d;
+  for (int l = 0; l < MAXD; ++l) {
+    p.m[l] = (l < d) ? n : 1;
+    p.n[l] = (l < d) ? n : 1;
+    p.ld[l] = (l < d) ? ld : 1;
+  }
+  p.Nx = p.Ny = p.sxw = N;
+}
+
+template <typename T>
+static int batched_impl(int d, int n, const T* A, T* X, T* Y, T* W, int batch, const kmx_options* opt,
+                        cudaStream_t s) {
+  if (d < 1 || d > MAXD || n < 1 || batch < 0) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!A || !X || !Y) return KMX_ERR_NULL_POINTER;
+  long long N;
+  if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  base_square(p, L_BATCHED, d, n, n, N);
+  p.count = batch;
+  p.A = A;
+  p.X = X;
+  p.Y = Y;
+  p.trans = o.transpose;
+  p.y_exclusive = 1;  // Y(:,k) are disjoint columns
+  if (W) {
+    p.wmode = 3;
+    p.Wbase = W;
+    p.w_stride = N;
+    p.nslots = batch;
+  }
+  return run_problem(p, sizeof(T) == 8, o, s);
+}
+
+template <typename T>
+static int pbatched_impl(int d, int n, const T* A, T* const* pX, T* const* pY, T* const* pW, int batch,
+                         const kmx_options* opt, cudaStream_t s) {
+  if (d < 1 || d > MAXD || n < 1 || batch < 0) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!A || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  long long N;
+  if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  base_square(p, L_PBATCHED, d, n, n, N);
+  p.count = batch;
+  p.A = A;
+  p.X = pX;
+  p.Y = const_cast<T**>(pY);
+  p.trans = o.transpose;
+  if (pW) {
+    p.wmode = 1;
+    p.pW = reinterpret_cast<void* const*>(pW);
+    p.nslots = batch;
+  }
+  return run_problem(p, sizeof(T) == 8, o, s);
+}
+
+template <typename T>
+static int xbatched_impl(int d, int n, const T* const* Aarray, int lda, T* const* pX, T* const* pY,
+                         T* const* pW, int batch, int sub, const kmx_options* opt, cudaStream_t s) {
+  if (d < 1 || d > MAXD || n < 1 || batch < 0 || sub < 0) return KMX_ERR_INVALID_ARG;
+  if (lda == 0) lda = n;
+  if (lda < n) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!Aarray || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  long long N;
+  if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  base_square(p, L_XBATCHED, d, n, lda, N);
+  p.count = batch;
+  p.A = Aarray;
+  p.X = pX;
+  p.Y = const_cast<T**>(pY);
+  p.trans = o.transpose;
+  if (pW) {
+    // Workspace slots exactly as the reference lays them out
+    // (kronmult_xbatched.hpp:121-126): pairs pW[2*iz], pW[2*iz+1] for
+    // iz < subbatchCount when batch > 1; pW[0] when batch == 1.
+    if (sub == 0) sub = (batch / 2 > 1) ? batch / 2 : 1;
+    if (batch > 1) {
+      p.wmode = 2;
+      p.nslots = sub;
+    } else {
+      p.wmode = 1;
+      p.nslots = 1;
+    }
+    p.pW = reinterpret_cast<void* const*>(pW);
+  }
+  return run_problem(p, sizeof(T) == 8, o, s);
+}
+
+template <typename T>
+static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarray, T* const* pX,
+                         T* const* pY, T* W, size_t Wcap, int batch, const kmx_options* opt,
+                         cudaStream_t s) {
+  if (d < 1 || d > MAXD || batch < 0 || !m || !n) return KMX_ERR_INVALID_ARG;
+  for (int l = 0; l < d; ++l)
+    if (m[l] < 1 || n[l] < 1) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!Aarray || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  std::memset(&p, 0, sizeof(p));
+  p.layout = L_VBATCHED;
+  p.d = d;
+  // applied operator: A_l (m x n), or A_l^T (n x m) when transposed
+  for (int l = 0; l < MAXD; ++l) {
+    const int ml = (l < d) ? m[l] : 1, nl = (l < d) ? n[l] : 1;
+    p.m[l] = o.transpose ? nl : ml;
+    p.n[l] = o.transpose ? ml : nl;
+    p.ld[l] = ml;  // the reference's vbatched uses ld = m (kronmult_vbatched.hpp:206-211)
+  }
+  long long Nx = 1, Ny = 1, sxw = 0;
+  for (int l = 0; l < d; ++l) {
+    Nx *= p.n[l];
+    Ny *= p.m[l];
+    if (Nx > (1LL << 31) - 1 || Ny > (1LL << 31) - 1) return KMX_ERR_UNSUPPORTED;
+  }
+  // largest intermediate m1..mk * n(k+1)..nd (kronmult_vbatched.hpp:136-153)
+  sxw = Nx;
+  for (int k = 1; k <= d; ++k) {
+    long long sz = 1;
+    for (int l = 0; l < k; ++l) sz *= p.m[l];
+    for (int l = k; l < d; ++l) sz *= p.n[l];
+    if (sz > sxw) sxw = sz;
+  }
+  p.Nx = Nx;
+  p.Ny = Ny;
+  p.sxw = sxw;
+  p.count = batch;
+  p.A = Aarray;
+  p.X = pX;
+  p.Y = const_cast<T**>(pY);
+  p.trans = o.transpose;
+  bool square = true;
+  for (int l = 0; l < d; ++l) square = square && (p.m[l] == p.n[0] && p.n[l] == p.n[0]);
+  if (!square) {
+    for (int l = 0; l < d; ++l)
+      if (p.m[l] == p.n[l] && p.n[l] > GEN_MAXN) return KMX_ERR_UNSUPPORTED;
+  }
+  if (W && Wcap > 0) {
+    const size_t slot_bytes = 2 * (size_t)sxw * sizeof(T);
+    p.wmode = 3;
+    p.Wbase = W;
+    p.w_stride = 2 * sxw;
+    p.nslots = (int)((Wcap / slot_bytes) < (size_t)batch ? (Wcap / slot_bytes) : (size_t)batch);
+  }
+  return run_problem(p, sizeof(T) == 8, o, s);
+}
+
+}  // namespace kmx
+
+using namespace kmx;
+
+#define KMX_STREAM(s) reinterpret_cast<cudaStream_t>(s)
+
+extern "C" {
+
+int kmx_kronmult_batched_f64(int d, int n, const double* A, double* X, double* Y, double* W,
+                             int batchCount, kmx_stream_t stream) {
+  return batched_impl<double>(d, n, A, X, Y, W, batchCount, nullptr, KMX_STREAM(stream));
+}
+int kmx_kronmult_batched_f64_ex(int d, int n, const double* A, double* X, double* Y, double* W,
+                                int batchCount, const kmx_options* opt, kmx_stream_t stream) {
+  return batched_impl<double>(d, n, A, X, Y, W, batchCount, opt, KMX_STREAM(stream));
+}
+int kmx_kronmult_batched_f32(int d, int n, const float* A, float* X, float* Y, float* W,
+                             int batchCount, kmx_stream_t stream) {
+  return batched_impl<float>(d, n, A, X, Y, W, batchCount, nullptr, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_pbatched_f64(int d, int n, const double* A, double* const* pX, double* const* pY,
+                              double* const* pW, int batchCount, kmx_stream_t stream) {
+  return pbatched_impl<double>(d, n, A, pX, pY, pW, batchCount, nullptr, KMX_STREAM(stream));
+}
+int kmx_kronmult_pbatched_f64_ex(int d, int n, const double* A, double* const* pX,
+                                 double* const* pY, double* const* pW, int batchCount,
+                                 const kmx_options* opt, kmx_stream_t stream) {
+  return pbatched_impl<double>(d, n, A, pX, pY, pW, batchCount, opt, KMX_STREAM(stream));
+}
+int kmx_kronmult_pbatched_f32(int d, int n, const float* A, float* const* pX, float* const* pY,
+                              float* const* pW, int batchCount, kmx_stream_t stream) {
+  return pbatched_impl<float>(d, n, A, pX, pY, pW, batchCount, nullptr, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_xbatched_f64(int d, int n, const double* const* Aarray, int lda,
+                              double* const* pX, double* const* pY, double* const* pW,
+                              int batchCount, int subbatchCount, kmx_stream_t stream) {
+  return xbatched_impl<double>(d, n, Aarray, lda, pX, pY, pW, batchCount, subbatchCount, nullptr,
+                               KMX_STREAM(stream));
+}
+int kmx_kronmult_xbatched_f64_ex(int d, int n, const double* const* Aarray, int lda,
+                                 double* const* pX, double* const* pY, double* const* pW,
+                                 int batchCount, int subbatchCount, const kmx_options* opt,
+                                 kmx_stream_t stream) {
+  return xbatched_impl<double>(d, n, Aarray, lda, pX, pY, pW, batchCount, subbatchCount, opt,
+                               KMX_STREAM(stream));
+}
+int kmx_kronmult_xbatched_f32(int d, int n, const float* const* Aarray, int lda, float* const* pX,
+                              float* const* pY, float* const* pW, int batchCount, int subbatchCount,
+                              kmx_stream_t stream) {
+  return xbatched_impl<float>(d, n, Aarray, lda, pX, pY, pW, batchCount, subbatchCount, nullptr,
+                              KMX_STREAM(stream));
+}
+
+int kmx_kronmult_vbatched_f64(int d, const int* m, const int* n, const double* const* Aarray,
+                              double* const* pX, double* const* pY, double* W,
+                              size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream) {
+  return vbatched_impl<double>(d, m, n, Aarray, pX, pY, W, Wcapacity_bytes, batchCount, nullptr,
+                               KMX_STREAM(stream));
+}
+int kmx_kronmult_vbatched_f64_ex(int d, const int* m, const int* n, const double* const* Aarray,
+                                 double* const* pX, double* const* pY, double* W,
+                                 size_t Wcapacity_bytes, int batchCount, const kmx_options* opt,
+                                 kmx_stream_t stream) {
+  return vbatched_impl<double>(d, m, n, Aarray, pX, pY, W, Wcapacity_bytes, batchCount, opt,
+                               KMX_STREAM(stream));
+}
+int kmx_kronmult_vbatched_f32(int d, const int* m, const int* n, const float* const* Aarray,
+                              float* const* pX, float* const* pY, float* W, size_t Wcapacity_bytes,
+                              int batchCount, kmx_stream_t stream) {
+  return vbatched_impl<float>(d, m, n, Aarray, pX, pY, W, Wcapacity_bytes, batchCount, nullptr,
+                              KMX_STREAM(stream));
+}
+
+void kmx_set_default_options(const kmx_options* opt) {
+  if (!opt) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  init_defaults_locked();
+  g_default = *opt;
+}
+
+void kmx_get_default_options(kmx_options* opt) {
+  if (!opt) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  init_defaults_locked();
+  *opt = g_default;
+}
+
+int kmx_check_device_status(kmx_stream_t stream, int* flags) {
+  int* sp = nullptr;
+  int rc = status_ptr(&sp);
+  if (rc != KMX_OK) return rc;
+  int host = 0;
+  cudaError_t e = cudaMemcpyAsync(&host, sp, sizeof(int), cudaMemcpyDeviceToHost, KMX_STREAM(stream));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(KMX_STREAM(stream));
+  if (e != cudaSuccess) return cuda_fail(e);
+  if (host != 0) {
+    const int zero = 0;
+    e = cudaMemcpyAsync(sp, &zero, sizeof(int), cudaMemcpyHostToDevice, KMX_STREAM(stream));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(KMX_STREAM(stream));
+    if (e != cudaSuccess) return cuda_fail(e);
+  }
+  if (flags) *flags = host;
+  return host ? KMX_ERR_DEVICE : KMX_OK;
+}
+
+int kmx_last_cuda_error(void) { return t_last_cuda_error; }
+
+const char* kmx_status_string(int status) {
+  switch (status) {
+    case KMX_OK: return "KMX_OK";
+    case KMX_ERR_INVALID_ARG: return "KMX_ERR_INVALID_ARG";
+    case KMX_ERR_NULL_POINTER: return "KMX_ERR_NULL_POINTER";
+    case KMX_ERR_WORKSPACE: return "KMX_ERR_WORKSPACE";
+    case KMX_ERR_UNSUPPORTED: return "KMX_ERR_UNSUPPORTED";
+    case KMX_ERR_CUDA: return "KMX_ERR_CUDA";
+    case KMX_ERR_DEVICE: return "KMX_ERR_DEVICE";
+    case KMX_ERR_OVERLAP: return "KMX_ERR_OVERLAP";
+    default: return "KMX_UNKNOWN_STATUS";
+  }
+}
+
+double kmx_kron_flops(int d, const int* m, const int* n) {
+  // kroncommon.hpp:204-234: level 1 costs 2*n2..nd*n1*m1, then m1 vectors recurse
+  if (d <= 0 || !m || !n) return 0.0;
+  if (d == 1) return 2.0 * m[0] * n[0];
+  double rest = 1.0;
+  for (int l = 1; l < d; ++l) rest *= n[l];
+  return 2.0 * rest * n[0] * m[0] + kmx_kron_flops(d - 1, m + 1, n + 1) * m[0];
+}
+
+const char* kmx_version(void) { return "kronmult-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,697 @@
+// kmx_engine.cuh -- device engine of the batched Kronecker mat-vec on sm_103a.
+//
+//   Y(:,k) += kron(A1(:,:,k), ..., Ad(:,:,k)) * X(:,k)
+//
+// One "entry" k is processed by a GROUP of G threads (G a multiple of 32);
+// a CTA holds E = blockDim/G groups, each with its own shared-memory region
+// and its own stream of entries (grid-stride over entries).  For one entry
+// the d mode contractions run on chip:
+//
+//   mode 0      reads the X block straight from HBM (the mode-0 fibers are
+//               the n slices of X, so lane f reads X[j*s + f]: coalesced) and
+//               writes the first intermediate to shared memory;
+//   modes 1..d-2 update the intermediate IN PLACE: a lane owns whole fibers
+//               (n elements at stride s), reads them, forms the n outputs and
+//               writes them back to the same slots;
+//   mode d-1    reads shared memory and adds its outputs to the Y block in
+//               HBM, one output per lane so consecutive lanes touch
+//               consecutive Y elements (coalesced FP64 atomics / RMW).
+//
+// The reference evaluates the same contractions in the same mode order (A1
+// first) as a recursion of tiny GEMMs with every intermediate in global
+// memory (kronmultv.hpp:19-148, kgemm_nt.hpp:215-385, kgemm_nn.hpp:227-406).
+//
+// Arithmetic forms:
+//   FormPlain<T>  T = double or float, fused multiply-add in T.
+//   FormSplit     FP64 in/out, carried as FP32 (hi, lo) pairs ("double-float"):
+//                 every product hi*hi is split exactly with an FMA, the sums of
+//                 hi parts are error-free (two-sum), the cross terms and the
+//                 errors are summed in FP32.  GB300 runs FP32 ~70x faster than
+//                 FP64, so this form trades ~2^-47 relative per operation for
+//                 ~6x throughput.  Each entry is first scaled by powers of two
+//                 (per factor and for X) so every carried value is <= 2 in
+//                 magnitude; the scale is folded back into the exponent of the
+//                 FP64 result.  Entries holding Inf/NaN take the plain path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace kmx {
+
+constexpr int MAXD = 6;
+constexpr int MAX_THREADS = 512;
+
+enum Layout : int { L_BATCHED = 0, L_PBATCHED = 1, L_XBATCHED = 2, L_VBATCHED = 3 };
+
+// Bits of the device status word.
+enum DevFlag : int { DF_NULL_PTR = 1, DF_WAIT_TIMEOUT = 2, DF_BAD_SHAPE = 4, DF_NONFINITE_SPLIT = 8 };
+
+// Everything a launch needs.  Shapes are those of the APPLIED operator:
+// mode l maps n[l] -> m[l]; with trans != 0 factor l is read transposed
+// (the host then passes m/n of A_l^T).
+struct Problem {
+  int layout;
+  int d;
+  int m[MAXD], n[MAXD], ld[MAXD];
+  long long Nx, Ny;      // input / output block lengths
+  long long sxw;         // largest intermediate (elements)
+  int count;             // entries in this launch
+  int entry_offset;      // index of the first entry (sub-batches)
+  const void* A;         // batched/pbatched: T base (n,n,d,batch); x/v: const T* const*
+  const void* X;         // batched: T base; otherwise T* const*
+  void* Y;               // batched: T base; otherwise T* const*
+  const int* order;      // optional processing order of entries (may be null)
+  int trans;             // read every factor transposed
+  int y_exclusive;       // Y blocks of distinct entries never overlap
+  int* status;           // device status word
+  // execution shape
+  int group_threads;     // G
+  int groups_per_cta;    // E
+  int group_smem;        // bytes of shared memory per group
+  // global-memory workspace for entries that do not fit on chip
+  int wmode;             // 0 none, 1 per-entry pointer array, 2 slot pointer pairs, 3 base+stride slots
+  void* const* pW;       // wmode 1: pW[entry]; wmode 2: pW[2*slot]
+  void* Wbase;           // wmode 3
+  long long w_stride;    // wmode 3: elements between slots
+  int nslots;            // concurrent workspace slots (grid*E must not exceed it)
+};
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+
+// Division by a run-time constant (round-up method), exact for n < 2^31.
+struct FastDiv {
+  unsigned mul;
+  int shift;
+  unsigned div;
+  __host__ __device__ FastDiv() : mul(1), shift(0), div(1) {}
+  __host__ __device__ explicit FastDiv(unsigned s) : div(s) {
+    shift = 0;
+    while ((1u << shift) < s) ++shift;
+    mul = (unsigned)(((1ull << 32) * ((1ull << shift) - s)) / s + 1);
+  }
+  __device__ __forceinline__ unsigned operator()(unsigned x) const {
+    return (__umulhi(mul, x) + x) >> shift;
+  }
+};
+
+__device__ __forceinline__ void group_sync(int g, int G) {
+  if (G == (int)blockDim.x) {
+    __syncthreads();
+  } else if (G == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(G) : "memory");
+  }
+}
+
+template <typename T>
+struct EntryPtrs {
+  const T* X;
+  T* Y;
+  const T* A[MAXD];
+  int ld[MAXD];
+};
+
+// Resolve the pointers of entry e.  Returns false if any is NULL.
+template <typename T>
+__device__ __forceinline__ bool resolve_entry(const Problem& p, long long e, EntryPtrs<T>& en) {
+  const int d = p.d;
+  if (p.layout == L_BATCHED || p.layout == L_PBATCHED) {
+    if (p.layout == L_BATCHED) {
+      en.X = static_cast<const T*>(p.X) + e * p.Nx;
+      en.Y = static_cast<T*>(p.Y) + e * p.Ny;
+    } else {
+      en.X = static_cast<T* const*>(p.X)[e];
+      en.Y = static_cast<T* const*>(p.Y)[e];
+    }
+    const long long nn = (long long)p.n[0] * p.n[0];
+#pragma unroll
+    for (int l = 0; l < MAXD; ++l) {
+      if (l < d) {
+        en.A[l] = static_cast<const T*>(p.A) + (e * d + l) * nn;
+        en.ld[l] = p.ld[l];
+      }
+    }
+  } else {
+    en.X = static_cast<T* const*>(p.X)[e];
+    en.Y = static_cast<T* const*>(p.Y)[e];
+    const T* const* Ap = static_cast<const T* const*>(p.A) + e * d;
+#pragma unroll
+    for (int l = 0; l < MAXD; ++l) {
+      if (l < d) {
+        en.A[l] = Ap[l];
+        en.ld[l] = p.ld[l];
+      }
+    }
+  }
+  bool ok = (en.X != nullptr) && (en.Y != nullptr);
+#pragma unroll
+  for (int l = 0; l < MAXD; ++l)
+    if (l < d) ok = ok && (en.A[l] != nullptr);
+  return ok;
+}
+
+// Global workspace of one group: two buffers of sxw elements (the second
+// only for rectangular shapes).  Returns false if none is available.
+template <typename T>
+__device__ __forceinline__ bool workspace(const Problem& p, long long entry, long long slot, T*& w0,
+                                          T*& w1) {
+  w0 = w1 = nullptr;
+  if (p.wmode == 1) {
+    w0 = static_cast<T*>(p.pW[entry]);
+  } else if (p.wmode == 2) {
+    w0 = static_cast<T*>(p.pW[2 * slot]);
+    w1 = static_cast<T*>(p.pW[2 * slot + 1]);
+  } else if (p.wmode == 3) {
+    w0 = static_cast<T*>(p.Wbase) + slot * p.w_stride;
+    w1 = w0 + p.sxw;
+  }
+  return w0 != nullptr;
+}
+
+template <typename T>
+__device__ __forceinline__ void y_accumulate(T* y, T v, bool exclusive) {
+  if (exclusive) {
+    *y += v;
+  } else {
+    atomicAdd(y, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Double-float ("split") arithmetic.  Explicit _rn intrinsics keep the
+// compiler from fusing the error-free transformations.
+// ---------------------------------------------------------------------------
+struct df {
+  float hi, lo;
+};
+
+// Biased FP64 exponent field of x (0 for zero/subnormal, 2047 for Inf/NaN).
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// Split x * 2^-(eref-1023) into (hi, lo) with integer operations only (no
+// FP64 pipe).  hi keeps the leading 24 significant bits (truncated), lo the
+// next 29 rounded to 24.  Values far below the scale (FP32 underflow) become
+// zero, which is below 2^-126 relative to the block's largest magnitude.
+__device__ __forceinline__ df split_scaled(double x, int eref) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int ef = (int)((b >> 52) & 0x7FF);
+  const int fe = ef - eref + 127;  // FP32 biased exponent of the scaled value
+  df r;
+  if (ef == 0 || fe <= 0) {
+    r.hi = 0.f;
+    r.lo = 0.f;
+    return r;
+  }
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  r.hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)(mant >> 29));
+  const unsigned rem = (unsigned)(mant & 0x1FFFFFFFu);
+  if (rem == 0) {
+    r.lo = 0.f;
+  } else {
+    // rem * 2^(fe-127-52): scale the FP32 value of rem by adding to its exponent.
+    const unsigned fb = __float_as_uint(__uint2float_rn(rem));
+    const int e2 = (int)((fb >> 23) & 0xFF) + fe - 179;
+    r.lo = (e2 > 0) ? __uint_as_float(sign | ((unsigned)e2 << 23) | (fb & 0x7FFFFFu)) : 0.f;
+  }
+  return r;
+}
+
+// Exact FP64 value of an FP32 number times 2^escale, by exponent arithmetic.
+// Normal-range results only; otherwise falls back to an FP64 multiply.
+__device__ __forceinline__ double f32_to_f64_scaled(float f, int escale) {
+  const unsigned u = __float_as_uint(f);
+  const int ef = (int)((u >> 23) & 0xFF);
+  if (ef == 0) return 0.0;  // zero, or an FP32 subnormal (negligible at this scale)
+  const int e = ef - 127 + 1023 + escale;
+  if (e <= 0 || e >= 2047) return (double)f * exp2((double)escale);
+  const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)e << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
+
+// sum_j a[j]*v[j] in double-float; the j = 0 term seeds the sums.
+template <int NN>
+__device__ __forceinline__ df df_dot(const df* a, const df* v) {
+  float s = __fmul_rn(a[0].hi, v[0].hi);
+  float c = __fmaf_rn(a[0].hi, v[0].hi, -s);
+  c = __fmaf_rn(a[0].hi, v[0].lo, c);
+  c = __fmaf_rn(a[0].lo, v[0].hi, c);
+#pragma unroll
+  for (int j = 1; j < NN; ++j) {
+    const float pr = __fmul_rn(a[j].hi, v[j].hi);
+    const float pe = __fmaf_rn(a[j].hi, v[j].hi, -pr);
+    const float t = __fadd_rn(s, pr);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, pe));
+    c = __fmaf_rn(a[j].hi, v[j].lo, c);
+    c = __fmaf_rn(a[j].lo, v[j].hi, c);
+  }
+  df r;
+  r.hi = __fadd_rn(s, c);
+  r.lo = __fsub_rn(c, __fsub_rn(r.hi, s));
+  return r;
+}
+
+// Same with a run-time length (generic path).
+__device__ __forceinline__ df df_dot_rt(const df* a, int astride, const df* v, long long vstride,
+                                        int nn) {
+  float s = __fmul_rn(a[0].hi, v[0].hi);
+  float c = __fmaf_rn(a[0].hi, v[0].hi, -s);
+  c = __fmaf_rn(a[0].hi, v[0].lo, c);
+  c = __fmaf_rn(a[0].lo, v[0].hi, c);
+  for (int j = 1; j < nn; ++j) {
+    const df aj = a[j * astride];
+    const df vj = v[j * vstride];
+    const float pr = __fmul_rn(aj.hi, vj.hi);
+    const float pe = __fmaf_rn(aj.hi, vj.hi, -pr);
+    const float t = __fadd_rn(s, pr);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, pe));
+    c = __fmaf_rn(aj.hi, vj.lo, c);
+    c = __fmaf_rn(aj.lo, vj.hi, c);
+  }
+  df r;
+  r.hi = __fadd_rn(s, c);
+  r.lo = __fsub_rn(c, __fsub_rn(r.hi, s));
+  return r;
+}
+
+
+// Factor rows of one mode: kept in registers when small enough (NN*NN
+// values of S), otherwise read from shared memory at each use.
+template <typename S, int NN>
+struct Rows {
+  static constexpr bool REG = (NN * NN * sizeof(S) <= 128);
+  S r[REG ? NN * NN : 1];
+  const S* s;
+  __device__ __forceinline__ void load(const S* src) {
+    s = src;
+    if constexpr (REG) {
+#pragma unroll
+      for (int i = 0; i < NN * NN; ++i) r[i] = src[i];
+    }
+  }
+  __device__ __forceinline__ const S* row(int a) const {
+    if constexpr (REG) {
+      return r + a * NN;
+    } else {
+      return s + a * NN;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Plain form, square factors, compile-time n = NN.
+// Shared memory per group: [d*NN*NN factor entries][N intermediates].
+// With GBUF the intermediate lives in a global workspace instead.
+// ---------------------------------------------------------------------------
+template <typename T, int NN, bool GBUF>
+__device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs<T>& en, T* sA,
+                                               T* buf, int lt, int G, int g) {
+  constexpr int NN2 = NN * NN;
+  const int d = p.d;
+  const int N = (int)p.Nx;
+  const int F = N / NN;  // fibers per mode
+  for (int i = lt; i < d * NN2; i += G) {
+    const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
+    const T* Al = en.A[l];
+    sA[i] = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
+  }
+  group_sync(g, G);
+  const bool excl = p.y_exclusive != 0;
+  if (d == 1) {
+    for (int i = lt; i < NN; i += G) {
+      T acc = sA[i * NN] * __ldg(en.X);
+#pragma unroll
+      for (int j = 1; j < NN; ++j) acc = fma(sA[i * NN + j], __ldg(en.X + j), acc);
+      y_accumulate(en.Y + i, acc, excl);
+    }
+    return;
+  }
+  // mode 0: X (HBM) -> buf.  Fibers f = 0..F-1 at stride F.
+  {
+    Rows<T, NN> a;
+    a.load(sA);
+    for (int f = lt; f < F; f += G) {
+      T v[NN];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) v[j] = __ldg(en.X + (long long)j * F + f);
+#pragma unroll
+      for (int r = 0; r < NN; ++r) {
+        const T* ar = a.row(r);
+        T acc = ar[0] * v[0];
+#pragma unroll
+        for (int j = 1; j < NN; ++j) acc = fma(ar[j], v[j], acc);
+        buf[(long long)r * F + f] = acc;
+      }
+    }
+  }
+  group_sync(g, G);
+  // modes 1..d-2 in place
+  int s = F / NN;
+  for (int k = 1; k < d - 1; ++k, s /= NN) {
+    Rows<T, NN> a;
+    a.load(sA + k * NN2);
+    const FastDiv fd((unsigned)s);
+    for (int f = lt; f < F; f += G) {
+      const unsigned o = fd((unsigned)f);
+      const int r0 = f - (int)o * s;
+      T* base = buf + (long long)o * NN * s + r0;
+      T v[NN];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) v[j] = base[(long long)j * s];
+#pragma unroll
+      for (int r = 0; r < NN; ++r) {
+        const T* ar = a.row(r);
+        T acc = ar[0] * v[0];
+#pragma unroll
+        for (int j = 1; j < NN; ++j) acc = fma(ar[j], v[j], acc);
+        base[(long long)r * s] = acc;
+      }
+    }
+    group_sync(g, G);
+  }
+  // last mode: buf -> Y, one output per lane (consecutive lanes, consecutive Y)
+  {
+    const T* Ad = sA + (d - 1) * NN2;
+    for (int i = lt; i < N; i += G) {
+      const int f = i / NN, r = i - f * NN;
+      const T* v = buf + (long long)f * NN;
+      T acc = Ad[r * NN] * v[0];
+#pragma unroll
+      for (int j = 1; j < NN; ++j) acc = fma(Ad[r * NN + j], v[j], acc);
+      y_accumulate(en.Y + i, acc, excl);
+    }
+  }
+}
+
+template <typename T, int NN, bool GBUF>
+__global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int G = p.group_threads;
+  const int E = p.groups_per_cta;
+  const int g = threadIdx.x / G;
+  const int lt = threadIdx.x - g * G;
+  if (g >= E) return;
+  constexpr int NN2 = NN * NN;
+  T* sA = reinterpret_cast<T*>(smem + (size_t)g * p.group_smem);
+  T* sbuf = sA + ((MAXD * NN2 * sizeof(T) + 15) / 16 * 16) / sizeof(T);
+  const long long slot0 = (long long)blockIdx.x * E + g;
+  const long long step = (long long)gridDim.x * E;
+  for (long long e = slot0; e < p.count; e += step) {
+    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+    EntryPtrs<T> en;
+    if (!resolve_entry<T>(p, entry, en)) {
+      if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    T* buf = sbuf;
+    if (GBUF) {
+      T* w1;
+      if (!workspace<T>(p, entry, slot0, buf, w1)) {
+        if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+        continue;
+      }
+    }
+    sq_plain_entry<T, NN, GBUF>(p, en, sA, buf, lt, G, g);
+    group_sync(g, G);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split (double-float) form, square factors, compile-time NN.  Same data flow
+// as the plain form; the shared intermediate holds (hi, lo) pairs.  An entry
+// whose inputs hold Inf/NaN is evaluated by the plain FP64 code instead.
+// ---------------------------------------------------------------------------
+template <int NN, bool GBUF>
+__global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int G = p.group_threads;
+  const int E = p.groups_per_cta;
+  const int g = threadIdx.x / G;
+  const int lt = threadIdx.x - g * G;
+  if (g >= E) return;
+  constexpr int NN2 = NN * NN;
+  const int d = p.d;
+  const int N = (int)p.Nx;
+  const int F = N / NN;
+  unsigned char* gbase = smem + (size_t)g * p.group_smem;
+  df* sA = reinterpret_cast<df*>(gbase);                        // d*NN2 pairs
+  int* sExp = reinterpret_cast<int*>(gbase + MAXD * NN2 * sizeof(df));  // MAXD+2 ints
+  unsigned char* sbuf_raw =
+      gbase + ((MAXD * NN2 * sizeof(df) + (MAXD + 2) * sizeof(int) + 15) / 16 * 16);
+  const long long slot0 = (long long)blockIdx.x * E + g;
+  const long long step = (long long)gridDim.x * E;
+  const bool excl = p.y_exclusive != 0;
+  for (long long e = slot0; e < p.count; e += step) {
+    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+    EntryPtrs<double> en;
+    if (!resolve_entry<double>(p, entry, en)) {
+      if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    unsigned char* bufp = sbuf_raw;
+    if (GBUF) {
+      double *w0, *w1;
+      if (!workspace<double>(p, entry, slot0, w0, w1)) {
+        if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+        continue;
+      }
+      bufp = reinterpret_cast<unsigned char*>(w0);
+    }
+    df* buf = reinterpret_cast<df*>(bufp);
+    // --- scales: max exponent field per factor and of X ---
+    if (lt < MAXD + 2) sExp[lt] = 0;
+    group_sync(g, G);
+    {
+      int emax[MAXD];
+#pragma unroll
+      for (int l = 0; l < MAXD; ++l) emax[l] = 0;
+      for (int i = lt; i < d * NN2; i += G) {
+        const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
+        const double* Al = en.A[l];
+        const double v = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
+        const int ef = exp_field(v);
+#pragma unroll
+        for (int q = 0; q < MAXD; ++q)
+          if (q == l) emax[q] = max(emax[q], ef);
+      }
+      int ex = 0;
+      for (int i = lt; i < N; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
+#pragma unroll
+      for (int l = 0; l < MAXD; ++l)
+        if (l < d && emax[l] > 0) atomicMax(&sExp[l], emax[l]);
+      if (ex > 0) atomicMax(&sExp[MAXD], ex);
+    }
+    group_sync(g, G);
+    int nonfinite = (sExp[MAXD] == 2047);
+    int escale = sExp[MAXD] - 1023;
+    for (int l = 0; l < d; ++l) {
+      nonfinite |= (sExp[l] == 2047);
+      escale += sExp[l] - 1023;
+    }
+    const bool zero_block = (sExp[MAXD] == 0);
+    bool anyzero = zero_block;
+    for (int l = 0; l < d; ++l) anyzero = anyzero || (sExp[l] == 0);
+    if (anyzero) {
+      // kron(...) X is exactly zero: nothing to add.
+      group_sync(g, G);
+      continue;
+    }
+    if (nonfinite) {
+      // Inf/NaN must propagate exactly as in FP64: evaluate with the plain form
+      // on the same (double-sized) buffer.
+      double* sAd = reinterpret_cast<double*>(gbase);
+      sq_plain_entry<double, NN, GBUF>(p, en, sAd, reinterpret_cast<double*>(bufp), lt, G, g);
+      group_sync(g, G);
+      continue;
+    }
+    // --- factors, scaled and split ---
+    for (int i = lt; i < d * NN2; i += G) {
+      const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
+      const double* Al = en.A[l];
+      const double v = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
+      sA[i] = split_scaled(v, sExp[l]);
+    }
+    const int ex = sExp[MAXD];
+    group_sync(g, G);
+    if (d == 1) {
+      for (int i = lt; i < NN; i += G) {
+        df v[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) v[j] = split_scaled(__ldg(en.X + j), ex);
+        const df o = df_dot<NN>(sA + i * NN, v);
+        const double y = f32_to_f64_scaled(o.hi, escale) + f32_to_f64_scaled(o.lo, escale);
+        y_accumulate(en.Y + i, y, excl);
+      }
+      group_sync(g, G);
+      continue;
+    }
+    // mode 0: X (HBM) -> buf
+    {
+      Rows<df, NN> a;
+      a.load(sA);
+      for (int f = lt; f < F; f += G) {
+        df v[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) v[j] = split_scaled(__ldg(en.X + (long long)j * F + f), ex);
+#pragma unroll
+        for (int r = 0; r < NN; ++r) buf[(long long)r * F + f] = df_dot<NN>(a.row(r), v);
+      }
+    }
+    group_sync(g, G);
+    int s = F / NN;
+    for (int k = 1; k < d - 1; ++k, s /= NN) {
+      Rows<df, NN> a;
+      a.load(sA + k * NN2);
+      const FastDiv fd((unsigned)s);
+      for (int f = lt; f < F; f += G) {
+        const unsigned o = fd((unsigned)f);
+        const int r0 = f - (int)o * s;
+        df* base = buf + (long long)o * NN * s + r0;
+        df v[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) v[j] = base[(long long)j * s];
+#pragma unroll
+        for (int r = 0; r < NN; ++r) base[(long long)r * s] = df_dot<NN>(a.row(r), v);
+      }
+      group_sync(g, G);
+    }
+    {
+      const df* Ad = sA + (d - 1) * NN2;
+      for (int i = lt; i < N; i += G) {
+        const int f = i / NN, r = i - f * NN;
+        df v[NN], a[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          v[j] = buf[(long long)f * NN + j];
+          a[j] = Ad[r * NN + j];
+        }
+        const df o = df_dot<NN>(a, v);
+        const double y = f32_to_f64_scaled(o.hi, escale) + f32_to_f64_scaled(o.lo, escale);
+        y_accumulate(en.Y + i, y, excl);
+      }
+    }
+    group_sync(g, G);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Generic path: run-time shapes (rectangular, or n without a compile-time
+// specialisation), plain form.  Square modes update the intermediate in
+// place (a lane owns whole fibers; n <= GEN_MAXN); a rectangular mode writes
+// the other of two buffers (sxw elements each).  Buffers are in shared
+// memory, or in the global workspace with GBUF.
+// Shared memory per group: [sum_l m_l*n_l factor entries][sxw][sxw if rectangular].
+// ---------------------------------------------------------------------------
+constexpr int GEN_MAXN = 64;
+
+template <typename T, bool GBUF>
+__global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int G = p.group_threads;
+  const int E = p.groups_per_cta;
+  const int g = threadIdx.x / G;
+  const int lt = threadIdx.x - g * G;
+  if (g >= E) return;
+  const int d = p.d;
+  int aoff[MAXD + 1];
+  aoff[0] = 0;
+#pragma unroll
+  for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
+  T* sA = reinterpret_cast<T*>(smem + (size_t)g * p.group_smem);
+  T* sb0 = sA + ((aoff[d] * sizeof(T) + 15) / 16 * 16) / sizeof(T);
+  T* sb1 = sb0 + ((p.sxw * sizeof(T) + 15) / 16 * 16) / sizeof(T);
+  const long long slot0 = (long long)blockIdx.x * E + g;
+  const long long step = (long long)gridDim.x * E;
+  const bool excl = p.y_exclusive != 0;
+  for (long long e = slot0; e < p.count; e += step) {
+    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+    EntryPtrs<T> en;
+    if (!resolve_entry<T>(p, entry, en)) {
+      if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    T* b0 = sb0;
+    T* b1 = sb1;
+    if (GBUF) {
+      if (!workspace<T>(p, entry, slot0, b0, b1)) {
+        if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+        continue;
+      }
+    }
+    for (int l = 0; l < d; ++l) {
+      const int ml = p.m[l], nl = p.n[l];
+      for (int i = lt; i < ml * nl; i += G) {
+        const int a = i / nl, j = i - a * nl;
+        sA[aoff[l] + i] = p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                  : en.A[l][a + (long long)j * en.ld[l]];
+      }
+    }
+    group_sync(g, G);
+    const T* src = en.X;
+    T* cur = b0;
+    unsigned outer = 1;
+    for (int k = 0; k < d; ++k) {
+      unsigned s = 1;
+      for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
+      const int mk = p.m[k], nk = p.n[k];
+      const T* Ak = sA + aoff[k];
+      const bool last = (k == d - 1);
+      if (!last && k > 0 && mk == nk) {
+        // square middle mode: in place on cur, one fiber per lane
+        const FastDiv fs(s);
+        const unsigned F = outer * s;
+        for (unsigned f = lt; f < F; f += G) {
+          const unsigned o = fs(f);
+          const unsigned r0 = f - o * s;
+          T* base = cur + (long long)o * nk * s + r0;
+          T v[GEN_MAXN];
+          for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
+          for (int a = 0; a < mk; ++a) {
+            T acc = Ak[a * nk] * v[0];
+            for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[j], acc);
+            base[(long long)a * s] = acc;
+          }
+        }
+      } else {
+        // out of place: one output element per lane
+        T* dst = last ? en.Y : ((k == 0) ? cur : (cur == b0 ? b1 : b0));
+        const FastDiv fs(s), fm((unsigned)mk);
+        const unsigned total = outer * (unsigned)mk * s;
+        for (unsigned q = lt; q < total; q += G) {
+          const unsigned t = fs(q);
+          const unsigned rr = q - t * s;
+          const unsigned o = fm(t);
+          const int a = (int)(t - o * (unsigned)mk);
+          const T* v = src + (long long)o * nk * s + rr;
+          T acc = Ak[a * nk] * v[0];
+          for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[(long long)j * s], acc);
+          if (last) {
+            y_accumulate(dst + q, acc, excl);
+          } else {
+            dst[q] = acc;
+          }
+        }
+        if (!last) cur = dst;
+      }
+      group_sync(g, G);
+      src = cur;
+      outer *= (unsigned)mk;
+    }
+  }
+}
+
+}  // namespace kmx

@@ -1,0 +1,11 @@
+// Per-form launchers, one translation unit each (compiled in parallel).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace kmx {
+struct Problem;
+struct LaunchHint;
+cudaError_t launch_f64_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
+cudaError_t launch_f64_split(Problem& p, const LaunchHint& h, cudaStream_t s);
+cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
+}  // namespace kmx

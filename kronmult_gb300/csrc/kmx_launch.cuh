@@ -1,0 +1,157 @@
+// kmx_launch.cuh -- host-side launch logic shared by the per-form translation
+// units: picks the kernel for a shape, sizes shared memory and the grid.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "kmx_engine.cuh"
+
+namespace kmx {
+
+enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2 };
+
+// Execution shape requested by the caller (0 = choose).
+struct LaunchHint {
+  int group_threads;
+  int groups_per_cta;
+  int max_ctas;  // cap on the grid (0 = fill the GPU)
+};
+
+struct DeviceInfo {
+  int sms = 0;
+  int max_smem_optin = 0;
+  int max_threads_per_sm = 0;
+};
+
+DeviceInfo device_info(int dev);
+// Raise a kernel's dynamic shared-memory limit once per (kernel, device).
+cudaError_t ensure_smem(const void* func, int dev, size_t bytes);
+
+inline size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+inline bool is_square(const Problem& p) {
+  for (int l = 0; l < p.d; ++l)
+    if (p.m[l] != p.n[0] || p.n[l] != p.n[0]) return false;
+  return true;
+}
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Threads per entry: about four work items per lane in the widest mode.
+inline int default_group_threads(long long N, int nn) {
+  long long items = N / (nn > 0 ? nn : 1);
+  long long g = (items + 3) / 4;
+  if (g < 32) g = 32;
+  if (g > 256) g = (N >= 16384) ? 512 : 256;
+  return round_up((int)g, 32);
+}
+
+template <typename T, int FORM, int NN, bool GB>
+const void* sq_kernel() {
+  if constexpr (FORM == FORM_SPLIT) {
+    return reinterpret_cast<const void*>(&sq_split_kernel<NN, GB>);
+  } else {
+    return reinterpret_cast<const void*>(&sq_plain_kernel<T, NN, GB>);
+  }
+}
+
+template <typename T, int FORM, bool GB>
+const void* pick_sq(int nn) {
+  switch (nn) {
+    case 2: return sq_kernel<T, FORM, 2, GB>();
+    case 3: return sq_kernel<T, FORM, 3, GB>();
+    case 4: return sq_kernel<T, FORM, 4, GB>();
+    case 5: return sq_kernel<T, FORM, 5, GB>();
+    case 6: return sq_kernel<T, FORM, 6, GB>();
+    case 7: return sq_kernel<T, FORM, 7, GB>();
+    case 8: return sq_kernel<T, FORM, 8, GB>();
+    case 16: return sq_kernel<T, FORM, 16, GB>();
+    default: return nullptr;
+  }
+}
+
+// Bytes of shared memory one group needs (on-chip intermediate included).
+template <typename T, int FORM>
+size_t sq_group_smem(const Problem& p, bool gbuf) {
+  const int nn = p.n[0];
+  size_t head = (FORM == FORM_SPLIT) ? align16(MAXD * nn * nn * 8 + (MAXD + 2) * sizeof(int))
+                                     : align16(MAXD * nn * nn * sizeof(T));
+  size_t buf = (p.d >= 2 && !gbuf) ? align16((size_t)p.Nx * (FORM == FORM_SPLIT ? 8 : sizeof(T))) : 0;
+  return head + buf;
+}
+
+template <typename T>
+size_t gen_group_smem(const Problem& p, bool gbuf) {
+  size_t fac = 0;
+  for (int l = 0; l < p.d; ++l) fac += (size_t)p.m[l] * p.n[l];
+  size_t head = align16(fac * sizeof(T));
+  if (gbuf || p.d < 2) return head;
+  // square modes work in place: one buffer; rectangular ones ping-pong: two
+  return head + (is_square(p) ? 1 : 2) * align16((size_t)p.sxw * sizeof(T));
+}
+
+// Launch one forward pass over p.count entries.  Returns cudaSuccess, or the
+// CUDA error of the launch; cudaErrorInvalidValue when the shape needs a
+// global workspace that p does not provide.
+template <typename T, int FORM>
+cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stream) {
+  if (p.count <= 0) return cudaSuccess;
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo di = device_info(dev);
+  const bool square = is_square(p);
+  const int nn = p.n[0];
+  const bool spec = square && pick_sq<T, FORM, false>(nn) != nullptr;
+  // FORM_SPLIT exists for specialised square shapes only; others run plain.
+  if (FORM == FORM_SPLIT && !spec) return cudaErrorNotSupported;
+
+  bool gbuf = false;
+  size_t gsm = spec ? sq_group_smem<T, FORM>(p, false) : gen_group_smem<T>(p, false);
+  if (gsm > (size_t)di.max_smem_optin) {
+    gbuf = true;
+    gsm = spec ? sq_group_smem<T, FORM>(p, true) : gen_group_smem<T>(p, true);
+    if (p.wmode == 0 || p.nslots <= 0) return cudaErrorInvalidValue;
+  }
+  const void* func = spec ? (gbuf ? pick_sq<T, FORM, true>(nn) : pick_sq<T, FORM, false>(nn))
+                          : (gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true>)
+                                  : reinterpret_cast<const void*>(&gen_plain_kernel<T, false>));
+
+  int G = hint.group_threads > 0 ? hint.group_threads : default_group_threads(p.Nx > p.Ny ? p.Nx : p.Ny, spec ? nn : 1);
+  if (G > MAX_THREADS) G = MAX_THREADS;
+  G = round_up(G, 32);
+  int E = hint.groups_per_cta > 0 ? hint.groups_per_cta : (256 / G > 0 ? 256 / G : 1);
+  if (gbuf) E = 1;
+  while (E > 1 && (size_t)E * gsm > (size_t)di.max_smem_optin) --E;
+  while (E > 1 && E * G > MAX_THREADS) --E;
+  // never more groups per CTA than entries
+  if (E > p.count) E = p.count;
+  const size_t smem = (size_t)E * gsm;
+  err = ensure_smem(func, dev, smem);
+  if (err != cudaSuccess) return err;
+
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, E * G, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) per_sm = 1;
+  long long want = ((long long)p.count + E - 1) / E;
+  long long cap = (long long)di.sms * per_sm;
+  if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
+  if (gbuf) {
+    long long slot_cap = p.nslots / E;
+    if (slot_cap < 1) return cudaErrorInvalidValue;
+    if (cap > slot_cap) cap = slot_cap;
+  }
+  const int grid = (int)(want < cap ? want : cap);
+
+  p.group_threads = G;
+  p.groups_per_cta = E;
+  p.group_smem = (int)gsm;
+  void* args[] = {&p};
+  return cudaLaunchKernel(func, dim3(grid), dim3(E * G), args, smem, stream);
+}
+
+}  // namespace kmx

@@ -1,0 +1,108 @@
+"""CPU tests of the C ABI: the library loads, exports every declared symbol,
+validates arguments before touching a GPU, and the C++ drop-in header
+compiles and links against it with the reference's signatures."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol(kmx):
+    from kronmult_gb300 import _lib
+
+    L = kmx.lib()
+    names = _lib.exported_symbols()
+    assert len(names) >= 19
+    for name in names:
+        assert hasattr(L, name), name
+
+
+def test_version_and_status_strings(kmx):
+    L = kmx.lib()
+    assert b"sm_103a" in L.kmx_version()
+    assert L.kmx_status_string(3) == b"KMX_ERR_WORKSPACE"
+
+
+@pytest.mark.parametrize("d,n,expect", [(0, 4, 1), (7, 4, 1), (3, 0, 1), (3, -2, 1)])
+def test_invalid_shape_rejected_without_gpu(kmx, d, n, expect):
+    L = kmx.lib()
+    assert L.kmx_kronmult_batched_f64(d, n, 8, 8, 8, 0, 4, None) == expect
+    assert L.kmx_kronmult_xbatched_f64(d, n, 8, 0, 8, 8, 0, 4, 0, None) == expect
+
+
+def test_null_pointers_and_empty_batch(kmx):
+    L = kmx.lib()
+    assert L.kmx_kronmult_batched_f64(3, 4, 0, 8, 8, 0, 4, None) == 2
+    assert L.kmx_kronmult_pbatched_f64(3, 4, 8, 0, 8, 0, 4, None) == 2
+    assert L.kmx_kronmult_xbatched_f64(3, 4, 8, 0, 0, 8, 0, 4, 0, None) == 2
+    # batchCount == 0 is a no-op, even with NULL arrays
+    assert L.kmx_kronmult_batched_f64(3, 4, 0, 0, 0, 0, 0, None) == 0
+    assert L.kmx_kronmult_xbatched_f32(6, 4, 0, 0, 0, 0, 0, 0, 0, None) == 0
+
+
+def test_lda_smaller_than_n_rejected(kmx):
+    L = kmx.lib()
+    assert L.kmx_kronmult_xbatched_f64(3, 4, 8, 3, 8, 8, 0, 2, 0, None) == 1
+    assert L.kmx_kronmult_xbatched_f64(3, 4, 8, 4, 8, 8, 0, 0, 0, None) == 0
+
+
+def test_vbatched_bad_shape_rejected(kmx):
+    L = kmx.lib()
+    m = (C.c_int * 3)(2, 0, 2)
+    n = (C.c_int * 3)(2, 2, 2)
+    assert L.kmx_kronmult_vbatched_f64(3, m, n, 8, 8, 8, 0, 0, 2, None) == 1
+
+
+def test_kron_flops_matches_reference_formula(kmx):
+    for d in range(1, 7):
+        for n in (1, 2, 3, 4, 8):
+            assert kmx.kron_flops(d, n) == 2.0 * d * n ** (d + 1)
+    # rectangular: kroncommon.hpp:204-234 recursion
+    assert kmx.kron_flops(2, [3, 2], [4, 5]) == 2.0 * 5 * 4 * 3 + 3 * (2.0 * 2 * 5)
+
+
+def test_default_options_roundtrip(kmx):
+    from kronmult_gb300 import _lib
+
+    L = kmx.lib()
+    old = _lib.Options()
+    L.kmx_get_default_options(C.byref(old))
+    try:
+        kmx.set_default_form("plain")
+        cur = _lib.Options()
+        L.kmx_get_default_options(C.byref(cur))
+        assert cur.form == 1 and cur.accumulate == 0
+    finally:
+        L.kmx_set_default_options(C.byref(old))
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
+def test_cpp_dropin_header_compiles_and_links(kmx, tmp_path):
+    """A translation unit written against the reference's host API (names,
+    argument order, default subbatchCount) builds against our header and
+    library without edits."""
+    src = tmp_path / "user.cpp"
+    src.write_text(r'''
+#include "kronmult_gb300.hpp"
+void user(int n, double* A, double** pA, double** pX, double** pY, double** pW, double* X,
+          double* Y, double* W, float* Af, float** pAf, float** pXf, float** pYf, float** pWf,
+          int batch) {
+  kronmult6_batched(n, A, X, Y, W, batch);
+  kronmult4_pbatched(n, A, pX, pY, pW, batch);
+  kronmult6_xbatched(n, pA, n + 3, pX, pY, pW, batch);
+  kronmult3_xbatched(n, pAf, n, pXf, pYf, pWf, batch, 8);
+  kronmult2_vbatched<double>(2, 3, 4, 5, pA, pX, pY, W, 1 << 20, batch);
+  kronmult6_vbatched<float>(1, 2, 2, 1, 1, 1, 2, 2, 3, 3, 2, 2, pAf, pXf, pYf, Af, 1 << 20, batch);
+}
+int main() { return 0; }
+''')
+    exe = tmp_path / "user"
+    lib_dir = os.path.join(ROOT, "kronmult_gb300")
+    subprocess.run(["g++", "-std=c++14", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), f"-L{lib_dir}", "-lkronmult_gb300",
+                    f"-Wl,-rpath,{lib_dir}"], check=True)
+    assert exe.exists()

@@ -1,0 +1,301 @@
+"""GPU parity of the CUDA path against the oracle and the golden vectors of the
+reference's own build.  Every call goes through the C ABI.
+
+Tolerances:
+  FP64 forms (plain and split): normwise relative error per Y block <= 1e-13.
+  FP32: the reference test's min(abs, rel) metric <= 1e-5
+        (test_kronmult6_xbatched.cpp:758) and normwise <= 2e-6.
+"""
+import numpy as np
+import pytest
+
+from tests.common import blockwise_rel_err, golden, ref_test_err, vb_cases
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+F64_TOL = 1e-13
+F32_TOL = 1e-5
+F32_NORM_TOL = 2e-6
+FORMS = ["plain", "split"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def check_status(kmx):
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+
+
+# ---------------------------------------------------------------------------
+# golden vectors (reference's own CPU build, ramp inputs of its tests)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d", range(1, 7))
+def test_batched_golden(kmx, oracle, form, d):
+    g = golden()
+    for n in (1, 2, 3, 4):
+        N = n ** d
+        for batch in (1, 3):
+            A = dev(oracle.ramp_a(n, d, batch))
+            X = dev(oracle.ramp_x(N, batch))
+            X0 = X.clone()
+            Y = torch.zeros_like(X)
+            W = torch.zeros_like(X)
+            kmx.kronmult_batched(d, n, A, X, Y, W, batch, form=form)
+            err = blockwise_rel_err(host(Y), g[f"batched_d{d}_n{n}_b{batch}"])
+            assert err <= F64_TOL, (n, batch, err)
+            assert torch.equal(X, X0)  # X is never modified
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d", range(1, 7))
+def test_pbatched_overlap_golden(kmx, oracle, form, d):
+    g = golden()
+    for n in (1, 2, 3, 4):
+        N = n ** d
+        batch = 4
+        X = dev(oracle.ramp_x(N, batch))
+        A = dev(oracle.ramp_a(n, d, batch))
+        Y = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+        W = torch.zeros_like(Y)
+        pX = kmx.pointer_array(X, [b * N for b in range(batch)])
+        pY = kmx.pointer_array(Y, [0] * batch)  # every entry accumulates into Y(:,1)
+        pW = kmx.pointer_array(W, [b * N for b in range(batch)])
+        kmx.kronmult_pbatched(d, n, A, pX, pY, pW, batch, form=form)
+        y = host(Y)
+        assert blockwise_rel_err(y[0], g[f"pbatched_d{d}_n{n}_b{batch}"]) <= F64_TOL
+        assert not y[1:].any()
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("form", FORMS + ["f32"])
+@pytest.mark.parametrize("d", range(1, 7))
+def test_xbatched_padded_lda_overlap_golden(kmx, oracle, form, d):
+    g = golden()
+    f32 = form == "f32"
+    T = np.float32 if f32 else np.float64
+    tag = "f32" if f32 else "f64"
+    for n in (1, 2, 3, 4):
+        N = n ** d
+        for batch in (1, 4):
+            lda = n + 3
+            Ab = dev(oracle.ramp_a(n, d, batch, lda=lda, dtype=T))
+            X = dev(oracle.ramp_x(N, batch, dtype=T))
+            X0 = X.clone()
+            Y = torch.zeros(N, dtype=X.dtype, device="cuda")
+            W = torch.zeros((max(batch, 2), N), dtype=X.dtype, device="cuda")
+            pA = kmx.pointer_array(Ab, [(b * d + l) * n * lda for b in range(batch) for l in range(d)])
+            pX = kmx.pointer_array(X, [b * N for b in range(batch)])
+            pY = kmx.pointer_array(Y, [0] * batch)
+            pW = kmx.pointer_array(W, [b * N for b in range(W.shape[0])])
+            kmx.kronmult_xbatched(d, n, pA, lda, pX, pY, pW, batch, dtype=X.dtype,
+                                  form=None if f32 else form)
+            y = host(Y)
+            ref = g[f"xbatched_{tag}_d{d}_n{n}_b{batch}"]
+            if f32:
+                assert ref_test_err(y, ref) <= F32_TOL
+                assert blockwise_rel_err(y, ref) <= F32_NORM_TOL
+            else:
+                assert blockwise_rel_err(y, ref) <= F64_TOL, (n, batch)
+            assert torch.equal(X, X0)
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("ci,d", vb_cases())
+@pytest.mark.parametrize("form", FORMS + ["f32"])
+def test_vbatched_rectangular_golden(kmx, ci, d, form):
+    g = golden()
+    m, nn = g[f"vbatched_c{ci}_m"], g[f"vbatched_c{ci}_n"]
+    A, X, Y0 = g[f"vbatched_c{ci}_A"], g[f"vbatched_c{ci}_X"], g[f"vbatched_c{ci}_Y0"]
+    f32 = form == "f32"
+    T = np.float32 if f32 else np.float64
+    batch, Nx = X.shape
+    Ny = Y0.shape[1]
+    fsz = [int(m[l] * nn[l]) for l in range(d)]
+    offs, o = [], 0
+    for b in range(batch):
+        for l in range(d):
+            offs.append(o)
+            o += fsz[l]
+    Ad, Xd, Yd = dev(A.astype(T)), dev(X.astype(T)), dev(Y0.astype(T))
+    pA = kmx.pointer_array(Ad, offs)
+    pX = kmx.pointer_array(Xd, [b * Nx for b in range(batch)])
+    pY = kmx.pointer_array(Yd, [b * Ny for b in range(batch)])
+    W = torch.zeros(1 << 16, dtype=Xd.dtype, device="cuda")
+    kmx.kronmult_vbatched(d, m, nn, pA, pX, pY, W, None, batch, dtype=Xd.dtype,
+                          form=None if f32 else form)
+    y = host(Yd)
+    ref = g[f"vbatched_{'f32' if f32 else 'f64'}_c{ci}"]
+    if f32:
+        assert ref_test_err(y, ref) <= F32_TOL
+    else:
+        assert blockwise_rel_err(y, ref) <= F64_TOL
+    check_status(kmx)
+
+
+# ---------------------------------------------------------------------------
+# random inputs against the oracle: larger n, accumulate into nonzero Y,
+# the shared-memory and the global-workspace paths
+# ---------------------------------------------------------------------------
+
+SHAPES = [(1, 7), (2, 9), (3, 8), (3, 16), (4, 5), (4, 8), (5, 4), (5, 6), (6, 2), (6, 3),
+          (6, 4), (6, 5), (2, 1), (4, 11), (5, 8)]
+
+
+@pytest.mark.parametrize("d,n", SHAPES)
+@pytest.mark.parametrize("form", FORMS)
+def test_batched_random_vs_oracle(kmx, oracle, d, n, form):
+    rng = np.random.default_rng(1000 * d + n)
+    N = n ** d
+    batch = 5 if N <= 40000 else 2
+    A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+    X = rng.standard_normal((batch, N))
+    Y0 = rng.uniform(-1, 1, (batch, N))
+    Yref = Y0.copy()
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Xd, Yd = dev(X), dev(Y0)
+    Wd = torch.zeros_like(Xd)
+    kmx.kronmult_batched(d, n, dev(A), Xd, Yd, Wd, batch, form=form)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (3, 16), (5, 3), (6, 8)])
+def test_f32_random_vs_oracle(kmx, oracle, d, n):
+    rng = np.random.default_rng(77 + d * n)
+    N = n ** d
+    batch = 4 if N <= 40000 else 2
+    A = (rng.standard_normal((batch, d, n, n)) / np.sqrt(n)).astype(np.float32)
+    X = rng.standard_normal((batch, N)).astype(np.float32)
+    Yref = np.zeros((batch, N), dtype=np.float32)
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Yd = torch.zeros((batch, N), dtype=torch.float32, device="cuda")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, torch.zeros_like(Yd), batch)
+    assert blockwise_rel_err(host(Yd), Yref) <= F32_NORM_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_xbatched_index_pool_vs_oracle(kmx, oracle, form):
+    """Pool layout of the benchmark, small: entries (y, x, a[d]) into shared
+    X/Y block pools and per-dimension factor pools, uneven Y counts."""
+    rng = np.random.default_rng(5)
+    d, n, pool, nx, ny, ne = 6, 4, 64, 40, 30, 500
+    N = n ** d
+    lda = n
+    Apool = rng.standard_normal((d, pool, n, n)) / 2
+    Xpool = rng.standard_normal((nx, N))
+    Y0 = rng.standard_normal((ny, N))
+    y_idx = rng.geometric(0.2, ne) % ny
+    x_idx = rng.integers(0, nx, ne)
+    a_idx = rng.integers(0, pool, (ne, d))
+    Yref = Y0.copy()
+    oracle.xbatched_idx(d, n, Apool, lda, pool, Xpool, Yref, y_idx, x_idx, a_idx)
+    Ad, Xd, Yd = dev(Apool), dev(Xpool), dev(Y0)
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xd, x_idx * N)
+    pY = kmx.pointer_array(Yd, y_idx * N)
+    kmx.kronmult_xbatched(d, n, pA, lda, pX, pY, None, ne, form=form)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d,n", [(3, 4), (6, 3), (2, 8)])
+def test_transpose_option(kmx, oracle, form, d, n):
+    """transpose=True applies kron(A1^T, ..., Ad^T): the backward dX product."""
+    rng = np.random.default_rng(9)
+    N = n ** d
+    batch = 3
+    A = rng.standard_normal((batch, d, n, n))
+    At = np.ascontiguousarray(np.swapaxes(A, 2, 3))
+    X = rng.standard_normal((batch, N))
+    Yref = np.zeros_like(X)
+    oracle.batched(d, n, At, X.copy(), Yref, np.zeros_like(X), batch)
+    Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form=form, transpose=True)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+
+
+def test_vbatched_large_rectangular_uses_workspace(kmx, oracle):
+    """d=5 with 8x7 factors: the entry exceeds shared memory, so the global
+    workspace slots of the reference's vbatched layout are used."""
+    rng = np.random.default_rng(11)
+    d = 5
+    m = [8, 7, 8, 7, 8]
+    nn = [7, 8, 7, 8, 8]
+    batch = 3
+    Nx, Ny = int(np.prod(nn)), int(np.prod(m))
+    fsz = [m[l] * nn[l] for l in range(d)]
+    A = rng.standard_normal(batch * sum(fsz))
+    X = rng.standard_normal((batch, Nx))
+    offs, o = [], 0
+    for b in range(batch):
+        row = []
+        for l in range(d):
+            row.append(o)
+            o += fsz[l]
+        offs.append(row)
+    Yref = np.zeros((batch, Ny))
+    sxw = oracle.size_xw(d, m, nn)
+    oracle.vbatched(d, m, nn, A, offs, X, [b * Nx for b in range(batch)], Yref,
+                    [b * Ny for b in range(batch)], np.zeros(2 * sxw * batch))
+    Ad, Xd = dev(A), dev(X)
+    Yd = torch.zeros((batch, Ny), dtype=torch.float64, device="cuda")
+    W = torch.zeros(2 * sxw * 2, dtype=torch.float64, device="cuda")  # two slots
+    kmx.kronmult_vbatched(d, m, nn, kmx.pointer_array(Ad, np.ravel(offs)),
+                          kmx.pointer_array(Xd, [b * Nx for b in range(batch)]),
+                          kmx.pointer_array(Yd, [b * Ny for b in range(batch)]), W, None, batch)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+# ---------------------------------------------------------------------------
+# error behaviour
+# ---------------------------------------------------------------------------
+
+def test_null_entry_pointer_sets_device_status(kmx):
+    """A NULL inside a device pointer array is skipped by the kernel and
+    reported through the status word (no fault)."""
+    d, n, batch = 3, 4, 4
+    N = n ** d
+    A = torch.rand((batch, d, n, n), dtype=torch.float64, device="cuda")
+    X = torch.rand((batch, N), dtype=torch.float64, device="cuda")
+    Y = torch.zeros_like(X)
+    pX = kmx.pointer_array(X, [b * N for b in range(batch)])
+    pX[2] = 0
+    pY = kmx.pointer_array(Y, [b * N for b in range(batch)])
+    kmx.kronmult_pbatched(d, n, A, pX, pY, None, batch)
+    torch.cuda.synchronize()
+    with pytest.raises(kmx.KmxError):
+        kmx.check_device_status()
+    y = Y.cpu().numpy()
+    assert not y[2].any() and y[0].any()
+    assert kmx.check_device_status() == 0  # cleared
+
+
+def test_missing_workspace_for_large_entry(kmx):
+    d, n, batch = 6, 8, 1
+    N = n ** d
+    A = torch.rand((batch, d, n, n), dtype=torch.float64, device="cuda")
+    X = torch.rand((batch, N), dtype=torch.float64, device="cuda")
+    Y = torch.zeros_like(X)
+    with pytest.raises(kmx.KmxError, match="WORKSPACE"):
+        kmx.kronmult_batched(d, n, A, X, Y, None, batch)
