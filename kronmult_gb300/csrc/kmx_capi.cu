@@ -113,6 +113,13 @@ cudaError_t ensure_smem(const void* func, int dev, size_t bytes) {
 // ---------------------------------------------------------------------------
 static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream_t s) {
   if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  // The generic kernel keeps one fiber of a square middle mode in a local
+  // array of GEN_MAXN elements; larger n has no code path.
+  const bool spec_n = (p.n[0] >= 2 && p.n[0] <= 8) || p.n[0] == 16;
+  if (!(is_square(p) && spec_n)) {
+    for (int k = 1; k < p.d - 1; ++k)
+      if (p.m[k] == p.n[k] && p.n[k] > GEN_MAXN) return KMX_ERR_UNSUPPORTED;
+  }
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
   LaunchHint h = {0, 0, 0};
@@ -122,8 +129,7 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   } else {
     int form = o.form;
     if (form == KMX_FORM_AUTO) {
-      const bool spec = is_square(p) && (p.n[0] >= 2 && p.n[0] <= 8 || p.n[0] == 16);
-      form = spec ? KMX_FORM_SPLIT : KMX_FORM_PLAIN;
+      form = (is_square(p) && spec_n) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN;
     }
     if (form == KMX_FORM_SPLIT) {
       e = launch_f64_split(p, h, s);
