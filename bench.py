@@ -1,0 +1,429 @@
+#!/usr/bin/env python
+"""Headline benchmark: FP64 xbatched kronmult, d=6, n=4, on one GB300.
+
+Workload (seeded synthetic, shapes and distributions of the reference's
+headline configuration): 8192 X blocks and 8192 Y blocks of n^d = 4096
+doubles, 131072 entries (y_idx, x_idx, a_idx[6]) with per-Y contribution
+counts geometric (mean 16, shuffled), x_idx uniform, factors drawn from a pool
+of 1024 4x4 matrices per dimension with entries N(0,1)/2, X ~ N(0,1).  The
+entries reach the library as the reference's xbatched pointer arrays
+(kronmult6_xbatched.cpp:5-13).  One step = one kronmult6_xbatched call over
+all entries.  X and Y pools are 256 MiB each (> 129 MB L2), so no L2 flush is
+needed between steps.
+
+Forms: "chosen" is the library's automatic choice for (d=6, n=4, FP64) -- the
+double-float split form; "plain" is native FP64.  Both are timed; the JSON
+line's value is the chosen form, and its error against the plain form is
+reported (the metric allows <= 1e-12).
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+D, NN, POOL, NBLOCKS, ENTRIES, MEAN_COUNT = 6, 4, 1024, 8192, 131072, 16
+SEED = 20261203
+WORKLOAD = "kronmult6_xbatched FP64 d=6 n=4, 131072 entries over 8192 X / 8192 Y blocks"
+METRIC = "kronmult GFLOP/s (FP64, xbatched d=6 n=4), chosen form vs plain at <=1e-12 rel err"
+
+
+def flops_per_entry(d=D, n=NN):
+    return 2.0 * d * n ** (d + 1)  # kron_flops, kroncommon.hpp:204-234
+
+
+def algorithmic_bytes(entries, nblocks, d=D, n=NN):
+    """X block + factors + 8 pointers read per entry; each Y block read and
+    written once."""
+    N = n ** d
+    return entries * (N * 8 + d * n * n * 8 + (d + 2) * 8) + nblocks * 2 * N * 8
+
+
+def make_workload(seed=SEED, entries=ENTRIES, nblocks=NBLOCKS, pool=POOL, d=D, n=NN):
+    rng = np.random.default_rng(seed)
+    counts = rng.geometric(1.0 / MEAN_COUNT, nblocks).astype(np.int64)
+    # adjust to exactly `entries`, keeping every count >= 1
+    diff = entries - int(counts.sum())
+    while diff != 0:
+        idx = rng.integers(0, nblocks, abs(diff))
+        if diff > 0:
+            np.add.at(counts, idx, 1)
+        else:
+            for i in idx:
+                if counts[i] > 1:
+                    counts[i] -= 1
+        diff = entries - int(counts.sum())
+    y_idx = np.repeat(np.arange(nblocks, dtype=np.int32), counts)
+    rng.shuffle(y_idx)
+    x_idx = rng.integers(0, nblocks, entries, dtype=np.int32)
+    a_idx = rng.integers(0, pool, (entries, d), dtype=np.int32)
+    N = n ** d
+    Apool = rng.standard_normal((d, pool, n, n)) / 2.0
+    Xpool = rng.standard_normal((nblocks, N))
+    return dict(y_idx=y_idx, x_idx=x_idx, a_idx=a_idx, Apool=Apool, Xpool=Xpool, counts=counts)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per entry of the split kernel from the committed ncu summary
+    (profiles/), or None."""
+    p = os.path.join(ROOT, "profiles", "xbatched_d6n4_traffic.txt")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_entry"):
+                    return float(line.split("=")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.2)
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        else:
+            self.out = ""
+
+    def summary(self):
+        rows = [r for r in csv.reader(io.StringIO(self.out)) if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle port of the reference's OpenMP path)
+# ---------------------------------------------------------------------------
+
+def cpu_rate(w, entries, reps=1):
+    """GFLOP/s of the oracle on the first `entries` entries (best of reps)."""
+    from oracle import pyoracle as po
+
+    Y = np.zeros_like(w["Xpool"])
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        po.xbatched_idx(D, NN, w["Apool"], NN, POOL, w["Xpool"], Y, w["y_idx"][:entries],
+                        w["x_idx"][:entries], w["a_idx"][:entries])
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return entries * flops_per_entry() / best / 1e9, best
+
+
+def cpu_baseline(w, budget_s=20.0):
+    from oracle import pyoracle as po
+
+    po.build(ref=False)
+    cores = po.max_threads()
+    rate0, t0 = cpu_rate(w, 2048)
+    entries = int(min(ENTRIES, max(2048, budget_s / 2 / max(t0, 1e-6) * 2048)))
+    rate, dt = cpu_rate(w, entries, reps=2)
+    return {"value": round(rate, 3), "unit": "GFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"first {entries} of the {ENTRIES} entries, best of 2 ({dt:.2f} s each), "
+                      f"oracle/kron_oracle.c OpenMP restatement of kronmult_xbatched.hpp"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (oracle port; the
+    reference's own build is x86-only here and cannot travel) on the host
+    cores, same workload and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as po
+
+    po.build(ref=False)
+    w = make_workload()
+    cores = po.max_threads()
+    _, t_small = cpu_rate(w, 2048)
+    per_entry = t_small / 2048
+    total_budget = 150.0
+    entries = int(min(ENTRIES, max(2048, total_budget / (args.steps + args.warmup) / per_entry)))
+    for _ in range(args.warmup):
+        cpu_rate(w, entries)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_rate(w, entries)
+        times.append(dt)
+    t = sum(times) / len(times)
+    val = entries * flops_per_entry() / t / 1e9
+    line = {
+        "metric": METRIC, "value": round(val, 3),
+        "unit": "GFLOP/s", "impl": "reference", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "entries_per_step": entries},
+        "cpu_baseline": {"value": round(val, 3), "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                         "sample": f"{entries} of {ENTRIES} entries per step"},
+        "e2e": {"value": round(val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    entries = args.entries
+    w = make_workload(seed=SEED + rank, entries=entries)
+    N = NN ** D
+    dev = torch.device("cuda", local)
+    Ad = torch.from_numpy(w["Apool"]).to(dev)
+    Xd = torch.from_numpy(w["Xpool"]).to(dev)
+    Yd = torch.zeros_like(Xd)
+    y_idx = torch.from_numpy(w["y_idx"]).to(dev).long()
+    x_idx = torch.from_numpy(w["x_idx"]).to(dev).long()
+    a_idx = torch.from_numpy(w["a_idx"]).to(dev).long()
+    lvl = torch.arange(D, device=dev).long()[None, :]
+
+    def ptrs(A, X, Y):
+        pA = ((lvl * POOL + a_idx) * (NN * NN * 8) + A.data_ptr()).reshape(-1).contiguous()
+        pX = x_idx * (N * 8) + X.data_ptr()
+        pY = y_idx * (N * 8) + Y.data_ptr()
+        return pA, pX, pY
+
+    pA, pX, pY = ptrs(Ad, Xd, Yd)
+    stream = torch.cuda.current_stream()
+
+    def step(form, Y_ptrs=pY):
+        kmx.kronmult_xbatched(D, NN, pA, NN, pX, Y_ptrs, None, entries, form=form)
+
+    def timed(form, K, W):
+        for _ in range(W):
+            step(form)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            step(form)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # plain FP64 first (untimed warm-up included), then the chosen form under clock sampling
+    ms_plain = timed("plain", max(2, args.steps // 2), max(1, args.warmup // 2))
+    with ClockSampler(local) as clk:
+        ms = timed("auto", args.steps, args.warmup)
+    clocks = clk.summary()
+    kmx.check_device_status()
+
+    # accuracy: chosen vs plain on a fresh Y, and both vs the oracle on a sample
+    Yc = torch.zeros_like(Xd)
+    Yp = torch.zeros_like(Xd)
+    _, _, pYc = ptrs(Ad, Xd, Yc)
+    _, _, pYp = ptrs(Ad, Xd, Yp)
+    step("auto", pYc)
+    step("plain", pYp)
+    torch.cuda.synchronize()
+    num = torch.linalg.vector_norm(Yc - Yp, dim=1)
+    den = torch.linalg.vector_norm(Yp, dim=1).clamp_min(1e-300)
+    err_vs_plain = float((num / den).max().item())
+
+    total_flops = entries * flops_per_entry() * world
+    value = total_flops / (ms * 1e-3) / 1e9
+    value_plain = total_flops / (ms_plain * 1e-3) / 1e9
+
+    # e2e through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        Ah = torch.from_numpy(w["Apool"]).pin_memory()
+        Xh = torch.from_numpy(w["Xpool"]).pin_memory()
+        Yh = torch.zeros_like(Xh).pin_memory()
+        Yout = torch.empty_like(Xh).pin_memory()
+        idx_h = torch.from_numpy(np.concatenate(
+            [w["y_idx"], w["x_idx"], w["a_idx"].ravel()]).astype(np.int32)).pin_memory()
+        A2, X2, Y2 = torch.empty_like(Ad), torch.empty_like(Xd), torch.empty_like(Xd)
+        idx_d = torch.empty(idx_h.numel(), dtype=torch.int32, device=dev)
+        h2d = (Ah.numel() + Xh.numel() + Yh.numel()) * 8 + idx_h.numel() * 4
+        d2h = Yh.numel() * 8
+
+        def e2e_step():
+            A2.copy_(Ah, non_blocking=True)
+            X2.copy_(Xh, non_blocking=True)
+            Y2.copy_(Yh, non_blocking=True)
+            idx_d.copy_(idx_h, non_blocking=True)
+            yi = idx_d[:entries].long()
+            xi = idx_d[entries:2 * entries].long()
+            ai = idx_d[2 * entries:].long().view(entries, D)
+            qA = ((lvl * POOL + ai) * (NN * NN * 8) + A2.data_ptr()).reshape(-1)
+            qX = xi * (N * 8) + X2.data_ptr()
+            qY = yi * (N * 8) + Y2.data_ptr()
+            kmx.kronmult_xbatched(D, NN, qA, NN, qX, qY, None, entries)
+            Yout.copy_(Y2, non_blocking=True)
+
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        K2 = max(3, args.steps // 2)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        f0.record(stream)
+        for _ in range(K2):
+            e2e_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / K2
+        ms_e2e = max(f0.elapsed_time(f1) / K2, wall * 1e3)
+        e2e = {"value": round(total_flops / (ms_e2e * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
+               "ms_per_step": round(ms_e2e, 3), "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peaks, peak_kind = load_peaks()
+    L = kmx.lib()
+    import ctypes as C
+
+    r64 = C.c_double(0)
+    r32 = C.c_double(0)
+    L.kmx_probe_fma_rate(1, C.byref(r64))
+    L.kmx_probe_fma_rate(0, C.byref(r32))
+    fp64_tflops = 2 * r64.value / 1e12
+    fp32_tflops = 2 * r32.value / 1e12
+    alg_bytes = algorithmic_bytes(entries, NBLOCKS)
+    achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
+    tpe = profile_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved_gbs / peaks["hbm_gbs"], 4),
+                "traffic": (round(tpe * entries) if tpe else None),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": int(alg_bytes)}
+    t_fp64 = total_flops / world / (fp64_tflops * 1e12)
+    t_hbm = alg_bytes / (peaks["hbm_gbs"] * 1e9)
+    north = {"definition": "max(flops / FP64 peak, bytes / HBM peak)",
+             "fp64_peak_tflops_measured": round(fp64_tflops, 3),
+             "fp32_peak_tflops_measured": round(fp32_tflops, 2),
+             "t_fp64_ms": round(t_fp64 * 1e3, 3), "t_hbm_ms": round(t_hbm * 1e3, 3),
+             "bound": "fp64" if t_fp64 > t_hbm else "hbm",
+             "frac_chosen": round(max(t_fp64, t_hbm) / (ms * 1e-3), 3),
+             "frac_plain": round(max(t_fp64, t_hbm) / (ms_plain * 1e-3), 3)}
+
+    cpu = None if args.no_cpu_baseline else cpu_baseline(w)
+    line = {
+        "metric": METRIC,
+        "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "d": D, "n": NN, "entries": entries,
+                   "x_blocks": NBLOCKS, "y_blocks": NBLOCKS, "factor_pool": POOL,
+                   "accumulate": "atomic", "form_chosen": "split (double-float)",
+                   "l2": "inputs larger than L2 (256 MiB X and Y pools), no flush",
+                   "seed": SEED, "parallelism": f"entries sharded per GPU x{world}"},
+        "plain": {"value": round(value_plain, 3), "unit": "GFLOP/s", "ms_per_step": round(ms_plain, 4)},
+        "rel_err_chosen_vs_plain": err_vs_plain,
+        "roofline": roofline, "north_star_roofline": north,
+        "gpu_launches": args.steps, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--entries", type=int, default=ENTRIES)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

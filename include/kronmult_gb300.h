@@ -150,6 +150,11 @@ const char* kmx_status_string(int status);
 /* Flops of one entry, 2 * sum over the recursion levels (kroncommon.hpp:204-234). */
 double kmx_kron_flops(int d, const int* m, const int* n);
 
+/* Measured fused multiply-add rate of the current device (FP64 when fp64 is
+ * nonzero, else FP32), in FMA per second, from a timed register-only loop.
+ * Used as the denominator of the compute roofline.  Synchronises the device. */
+int kmx_probe_fma_rate(int fp64, double* fma_per_second);
+
 /* Version string of this build. */
 const char* kmx_version(void);
 

@@ -67,6 +67,7 @@ _SIGS = {
     "kmx_kronmult_vbatched_f64_ex": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _optp, _vp],
     "kmx_check_device_status": [_vp, _ip],
     "kmx_last_cuda_error": [],
+    "kmx_probe_fma_rate": [_i, C.POINTER(C.c_double)],
     "kmx_set_default_options": [_optp],
     "kmx_get_default_options": [_optp],
 }

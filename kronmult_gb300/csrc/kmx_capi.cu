@@ -122,7 +122,12 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   }
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
-  LaunchHint h = {0, 0, 0};
+  LaunchHint h = {0, 0, 0, 0};
+  static const int engine_env = [] {
+    const char* e = std::getenv("KMX_ENGINE");
+    return e ? std::atoi(e) : 0;
+  }();
+  h.engine = engine_env;
   cudaError_t e;
   if (!is_f64) {
     e = launch_f32_plain(p, h, s);

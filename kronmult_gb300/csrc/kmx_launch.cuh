@@ -8,6 +8,7 @@
 #include <unordered_map>
 
 #include "kmx_engine.cuh"
+#include "kmx_tile.cuh"
 
 namespace kmx {
 
@@ -18,6 +19,7 @@ struct LaunchHint {
   int group_threads;
   int groups_per_cta;
   int max_ctas;  // cap on the grid (0 = fill the GPU)
+  int engine;    // 0 choose, 1 per-mode kernels only, 2 register-tiled kernels only
 };
 
 struct DeviceInfo {
@@ -73,6 +75,92 @@ const void* pick_sq(int nn) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-tiled kernels (kmx_tile.cuh) for square NN in 2..8, d in 3..6,
+// where one entry's intermediate fits in shared memory.
+// ---------------------------------------------------------------------------
+template <typename T, int FORM>
+struct TilePol {
+  using type = tile::PlainPolicy<T>;
+};
+template <typename T>
+struct TilePol<T, FORM_SPLIT> {
+  using type = tile::SplitPolicy;
+};
+
+struct TileKernel {
+  const void* func = nullptr;
+  int group_threads = 0;
+  int group_smem = 0;
+};
+
+template <typename T, int FORM, int NN, int D>
+TileKernel tile_entry() {
+  using Pol = typename TilePol<T, FORM>::type;
+  TileKernel k;
+  constexpr int bytes = tile::group_smem_bytes<Pol, NN, D>();
+  if constexpr (bytes <= 227 * 1024) {
+    k.func = reinterpret_cast<const void*>(&tile::tile_kernel<Pol, NN, D>);
+    k.group_threads = tile::group_threads(NN, D);
+    k.group_smem = bytes;
+  }
+  return k;
+}
+
+template <typename T, int FORM, int NN>
+TileKernel tile_for_d(int d) {
+  switch (d) {
+    case 3: return tile_entry<T, FORM, NN, 3>();
+    case 4: return tile_entry<T, FORM, NN, 4>();
+    case 5: return tile_entry<T, FORM, NN, 5>();
+    case 6: return tile_entry<T, FORM, NN, 6>();
+    default: return TileKernel();
+  }
+}
+
+template <typename T, int FORM>
+TileKernel pick_tile(int nn, int d) {
+  switch (nn) {
+    case 2: return tile_for_d<T, FORM, 2>(d);
+    case 3: return tile_for_d<T, FORM, 3>(d);
+    case 4: return tile_for_d<T, FORM, 4>(d);
+    case 5: return tile_for_d<T, FORM, 5>(d);
+    case 6: return tile_for_d<T, FORM, 6>(d);
+    case 7: return tile_for_d<T, FORM, 7>(d);
+    case 8: return tile_for_d<T, FORM, 8>(d);
+    default: return TileKernel();
+  }
+}
+
+// Launch a register-tiled kernel; grid fills the GPU by occupancy.
+inline cudaError_t launch_tile(Problem& p, const TileKernel& k, const LaunchHint& hint,
+                               cudaStream_t stream) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo di = device_info(dev);
+  const int G = k.group_threads;
+  int E = hint.groups_per_cta > 0 ? hint.groups_per_cta : (G >= 256 ? 1 : 256 / G);
+  while (E > 1 && (size_t)E * k.group_smem > (size_t)di.max_smem_optin) --E;
+  if (E > p.count) E = p.count;
+  const size_t smem = (size_t)E * k.group_smem;
+  err = ensure_smem(k.func, dev, smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.func, E * G, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const long long want = ((long long)p.count + E - 1) / E;
+  long long cap = (long long)di.sms * per_sm;
+  if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
+  const int grid = (int)(want < cap ? want : cap);
+  p.group_threads = G;
+  p.groups_per_cta = E;
+  p.group_smem = k.group_smem;
+  void* args[] = {&p};
+  return cudaLaunchKernel(k.func, dim3(grid), dim3(E * G), args, smem, stream);
+}
+
 // Bytes of shared memory one group needs (on-chip intermediate included).
 template <typename T, int FORM>
 size_t sq_group_smem(const Problem& p, bool gbuf) {
@@ -105,6 +193,10 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   const DeviceInfo di = device_info(dev);
   const bool square = is_square(p);
   const int nn = p.n[0];
+  if (square && hint.engine != 1) {
+    const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
+    if (tk.func) return launch_tile(p, tk, hint, stream);
+  }
   const bool spec = square && pick_sq<T, FORM, false>(nn) != nullptr;
   // FORM_SPLIT exists for specialised square shapes only; others run plain.
   if (FORM == FORM_SPLIT && !spec) return cudaErrorNotSupported;

@@ -299,3 +299,43 @@ def test_missing_workspace_for_large_entry(kmx):
     Y = torch.zeros_like(X)
     with pytest.raises(kmx.KmxError, match="WORKSPACE"):
         kmx.kronmult_batched(d, n, A, X, Y, None, batch)
+
+
+@pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (5, 3), (3, 5)])
+def test_split_form_extreme_magnitudes(kmx, oracle, d, n):
+    """Factors and X spanning 1e-200..1e200: the split form rescales every
+    entry by powers of two, so its FP32 carriers never overflow or flush."""
+    rng = np.random.default_rng(21)
+    N = n ** d
+    batch = 4
+    A = rng.standard_normal((batch, d, n, n))
+    A *= 10.0 ** rng.integers(-200, 200, (batch, d, 1, 1))
+    X = rng.standard_normal((batch, N)) * 10.0 ** rng.integers(-150, 150, (batch, 1))
+    Yref = np.zeros_like(X)
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split")
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_nonfinite_inputs_propagate_like_fp64(kmx, oracle, form):
+    """Inf/NaN in X or a factor propagate exactly as in FP64 arithmetic (the
+    split form evaluates such entries with native FP64)."""
+    rng = np.random.default_rng(22)
+    d, n, batch = 6, 4, 4
+    N = n ** d
+    A = rng.standard_normal((batch, d, n, n))
+    X = rng.standard_normal((batch, N))
+    X[1, 77] = np.inf
+    A[2, 3, 1, 2] = np.nan
+    Yref = np.zeros_like(X)
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form=form)
+    y = host(Yd)
+    assert np.array_equal(np.isnan(y), np.isnan(Yref))
+    assert np.array_equal(np.isinf(y), np.isinf(Yref))
+    fin = np.isfinite(Yref).all(axis=1)
+    assert blockwise_rel_err(y[fin], Yref[fin]) <= F64_TOL
