@@ -39,7 +39,8 @@ typedef enum kmx_status {
   KMX_ERR_UNSUPPORTED = 4,   /* shape or option this build does not handle */
   KMX_ERR_CUDA = 5,          /* a CUDA runtime call failed (see kmx_last_cuda_error) */
   KMX_ERR_DEVICE = 6,        /* a kernel reported an error through the device status word */
-  KMX_ERR_OVERLAP = 7        /* deterministic mode: Y blocks partially overlap */
+  KMX_ERR_OVERLAP = 7        /* deterministic mode: Y blocks partially overlap (reported
+                                through the device status word, bit 16) */
 } kmx_status;
 
 /* Arithmetic form of the FP64 entry points. */
@@ -57,10 +58,24 @@ typedef enum kmx_accumulate {
                                 in a fixed order and written once: bitwise reproducible */
 } kmx_accumulate;
 
+/* Kernel family for square factors. */
+typedef enum kmx_engine {
+  KMX_ENGINE_TUNED = 0,    /* the committed tuning table's choice for (form, d, n) */
+  KMX_ENGINE_PER_MODE = 1, /* one mode contraction per pass over shared memory */
+  KMX_ENGINE_TILED = 2     /* register tiles of one or two modes, TMA-prefetched X */
+} kmx_engine;
+
 typedef struct kmx_options {
   int form;        /* kmx_form */
   int accumulate;  /* kmx_accumulate */
   int transpose;   /* nonzero: use A_l^T for every factor (the backward dX product) */
+  int engine;      /* kmx_engine */
+  /* Deterministic mode only: device workspace of at least
+   * kmx_deterministic_workspace_bytes(batchCount) bytes.  NULL: the library
+   * keeps one stream-ordered workspace per device (cudaMallocAsync on first
+   * use and on growth), which calls on different streams must not share. */
+  void* workspace;
+  size_t workspace_bytes;
 } kmx_options;
 
 /* ---------------------------------------------------------------------- */
@@ -127,6 +142,20 @@ int kmx_kronmult_vbatched_f64_ex(int d, const int* m, const int* n,
                                  double* const* pY, double* W, size_t Wcapacity_bytes,
                                  int batchCount, const kmx_options* opt, kmx_stream_t stream);
 
+int kmx_kronmult_batched_f32_ex(int d, int n, const float* A, float* X, float* Y, float* W,
+                                int batchCount, const kmx_options* opt, kmx_stream_t stream);
+int kmx_kronmult_pbatched_f32_ex(int d, int n, const float* A, float* const* pX, float* const* pY,
+                                 float* const* pW, int batchCount, const kmx_options* opt,
+                                 kmx_stream_t stream);
+int kmx_kronmult_xbatched_f32_ex(int d, int n, const float* const* Aarray, int lda,
+                                 float* const* pX, float* const* pY, float* const* pW,
+                                 int batchCount, int subbatchCount, const kmx_options* opt,
+                                 kmx_stream_t stream);
+int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float* const* Aarray,
+                                 float* const* pX, float* const* pY, float* W,
+                                 size_t Wcapacity_bytes, int batchCount, const kmx_options* opt,
+                                 kmx_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Library state and diagnostics.                                          */
 /* ---------------------------------------------------------------------- */
@@ -134,6 +163,13 @@ int kmx_kronmult_vbatched_f64_ex(int d, const int* m, const int* n,
 /* Default options used by the drop-in entry points (process-wide). */
 void kmx_set_default_options(const kmx_options* opt);
 void kmx_get_default_options(kmx_options* opt);
+
+/* Device workspace the deterministic mode needs for batchCount entries. */
+size_t kmx_deterministic_workspace_bytes(int batchCount);
+
+/* Frees the library's cached deterministic-mode workspace of the current
+ * device (stream-ordered on the given stream). */
+int kmx_release_workspace(kmx_stream_t stream);
 
 /* Reads and clears the current device's status word, written by kernels
  * that met a NULL pointer inside a pointer array or a wait that ran out.

@@ -94,14 +94,15 @@ def check_device_status(stream=None) -> int:
     return flags.value
 
 
-def _opt(form, accumulate, transpose):
-    if form is None and accumulate is None and not transpose:
+def _opt(form, accumulate, transpose, engine=None, workspace=None):
+    if form is None and accumulate is None and not transpose and engine is None:
         return None
-    return C.byref(options(form or "auto", accumulate or "atomic", transpose))
+    o = options(form or "auto", accumulate or "atomic", transpose, engine or "tuned")
+    return C.byref(o)
 
 
 def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accumulate=None,
-                     transpose=False, stream=None):
+                     transpose=False, engine=None, stream=None):
     """kronmult{d}_batched: A (n,n,d,batch) column-major, X/Y/W (n^d, batch)."""
     f64 = _is_f64(A.dtype)
     b = batchCount if batchCount is not None else X.numel() // (n ** d)
@@ -109,16 +110,17 @@ def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accum
     L = lib()
     if f64:
         rc = L.kmx_kronmult_batched_f64_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
-                                           _opt(form, accumulate, transpose), s)
+                                           _opt(form, accumulate, transpose, engine), s)
     else:
-        if form not in (None, "auto", "plain") or transpose or accumulate not in (None, "atomic"):
+        if form not in (None, "auto", "plain"):
             raise KmxError(4, "kmx_kronmult_batched_f32")
-        rc = L.kmx_kronmult_batched_f32(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b, s)
+        rc = L.kmx_kronmult_batched_f32_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
+                                           _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_batched")
 
 
 def kronmult_pbatched(d, n, A, pX, pY, pW=None, batchCount=None, *, form=None, accumulate=None,
-                      transpose=False, stream=None):
+                      transpose=False, engine=None, stream=None):
     """kronmult{d}_pbatched: A (n,n,d,batch); pX/pY/pW int64 address tensors."""
     f64 = _is_f64(A.dtype)
     b = batchCount if batchCount is not None else pX.numel()
@@ -126,14 +128,16 @@ def kronmult_pbatched(d, n, A, pX, pY, pW=None, batchCount=None, *, form=None, a
     L = lib()
     if f64:
         rc = L.kmx_kronmult_pbatched_f64_ex(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b,
-                                            _opt(form, accumulate, transpose), s)
+                                            _opt(form, accumulate, transpose, engine), s)
     else:
-        rc = L.kmx_kronmult_pbatched_f32(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b, s)
+        rc = L.kmx_kronmult_pbatched_f32_ex(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b,
+                                            _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_pbatched")
 
 
 def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subbatchCount=0, *,
-                      dtype=None, form=None, accumulate=None, transpose=False, stream=None):
+                      dtype=None, form=None, accumulate=None, transpose=False, engine=None,
+                      stream=None):
     """kronmult{d}_xbatched: Aarray (d, batch) factor addresses with leading
     dimension lda; pX/pY/pW address arrays.  dtype is float64 unless given."""
     t = _torch()
@@ -144,15 +148,17 @@ def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subba
     if f64:
         rc = L.kmx_kronmult_xbatched_f64_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
                                             _addr(pW), b, subbatchCount,
-                                            _opt(form, accumulate, transpose), s)
+                                            _opt(form, accumulate, transpose, engine), s)
     else:
-        rc = L.kmx_kronmult_xbatched_f32(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
-                                         _addr(pW), b, subbatchCount, s)
+        rc = L.kmx_kronmult_xbatched_f32_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
+                                            _addr(pW), b, subbatchCount,
+                                            _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_xbatched")
 
 
 def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, batchCount=None, *,
-                      dtype=None, form=None, accumulate=None, transpose=False, stream=None):
+                      dtype=None, form=None, accumulate=None, transpose=False, engine=None,
+                      stream=None):
     """kronmult{d}_vbatched: factor l is m[l] x n[l] (ld = m[l]) for every entry."""
     t = _torch()
     f64 = _is_f64(dtype if dtype is not None else t.float64)
@@ -165,10 +171,10 @@ def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, bat
     L = lib()
     if f64:
         rc = L.kmx_kronmult_vbatched_f64_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
-                                            _addr(W), cap, b, _opt(form, accumulate, transpose), s)
+                                            _addr(W), cap, b, _opt(form, accumulate, transpose, engine), s)
     else:
-        rc = L.kmx_kronmult_vbatched_f32(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY), _addr(W),
-                                         cap, b, s)
+        rc = L.kmx_kronmult_vbatched_f32_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
+                                            _addr(W), cap, b, _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_vbatched")
 
 

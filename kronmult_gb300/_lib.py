@@ -28,6 +28,7 @@ STATUS = {
 }
 
 FORMS = {"auto": 0, "plain": 1, "split": 2}
+ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2}
 ACCUMULATE = {"atomic": 0, "deterministic": 1}
 
 
@@ -42,7 +43,8 @@ class KmxError(RuntimeError):
 
 
 class Options(C.Structure):
-    _fields_ = [("form", C.c_int), ("accumulate", C.c_int), ("transpose", C.c_int)]
+    _fields_ = [("form", C.c_int), ("accumulate", C.c_int), ("transpose", C.c_int),
+                ("engine", C.c_int), ("workspace", C.c_void_p), ("workspace_bytes", C.c_size_t)]
 
 
 _vp = C.c_void_p
@@ -65,9 +67,14 @@ _SIGS = {
     "kmx_kronmult_vbatched_f64": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _vp],
     "kmx_kronmult_vbatched_f32": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _vp],
     "kmx_kronmult_vbatched_f64_ex": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _optp, _vp],
+    "kmx_kronmult_batched_f32_ex": [_i, _i, _vp, _vp, _vp, _vp, _i, _optp, _vp],
+    "kmx_kronmult_pbatched_f32_ex": [_i, _i, _vp, _vp, _vp, _vp, _i, _optp, _vp],
+    "kmx_kronmult_xbatched_f32_ex": [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _optp, _vp],
+    "kmx_kronmult_vbatched_f32_ex": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _optp, _vp],
     "kmx_check_device_status": [_vp, _ip],
     "kmx_last_cuda_error": [],
     "kmx_probe_fma_rate": [_i, C.POINTER(C.c_double)],
+    "kmx_release_workspace": [_vp],
     "kmx_set_default_options": [_optp],
     "kmx_get_default_options": [_optp],
 }
@@ -101,6 +108,8 @@ def lib():
             L.kmx_kron_flops.restype = C.c_double
             L.kmx_status_string.argtypes = [_i]
             L.kmx_status_string.restype = C.c_char_p
+            L.kmx_deterministic_workspace_bytes.argtypes = [_i]
+            L.kmx_deterministic_workspace_bytes.restype = C.c_size_t
             L.kmx_version.argtypes = []
             L.kmx_version.restype = C.c_char_p
             _lib = L
@@ -112,7 +121,9 @@ def check(status: int, where: str) -> None:
         raise KmxError(status, where)
 
 
-def options(form: str | int = "auto", accumulate: str | int = "atomic", transpose: bool = False):
+def options(form: str | int = "auto", accumulate: str | int = "atomic", transpose: bool = False,
+            engine: str | int = "tuned"):
     f = FORMS[form] if isinstance(form, str) else int(form)
     a = ACCUMULATE[accumulate] if isinstance(accumulate, str) else int(accumulate)
-    return Options(f, a, 1 if transpose else 0)
+    g = ENGINES[engine] if isinstance(engine, str) else int(engine)
+    return Options(f, a, 1 if transpose else 0, g, None, 0)

@@ -10,6 +10,7 @@
 #include "../../include/kronmult_gb300.h"
 #include "kmx_forms.h"
 #include "kmx_launch.cuh"
+#include "kmx_segments.h"
 
 namespace kmx {
 
@@ -29,7 +30,11 @@ bool g_dev_ok[MAX_DEVICES];
 int* g_status_ptr[MAX_DEVICES];
 std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 
-kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0};
+kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
+
+// Library-owned deterministic-mode workspace, one per device, stream ordered.
+void* g_ws_ptr[MAX_DEVICES];
+size_t g_ws_bytes[MAX_DEVICES];
 bool g_default_init = false;
 
 void init_defaults_locked() {
@@ -81,6 +86,28 @@ bool ipow_checked(int n, int d, long long* out) {
   return true;
 }
 
+int cached_workspace(size_t need, cudaStream_t s, void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e);
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_ws_bytes[dev] < need) {
+    if (g_ws_ptr[dev]) {
+      e = cudaFreeAsync(g_ws_ptr[dev], s);
+      if (e != cudaSuccess) return cuda_fail(e);
+      g_ws_ptr[dev] = nullptr;
+      g_ws_bytes[dev] = 0;
+    }
+    void* p = nullptr;
+    e = cudaMallocAsync(&p, need, s);
+    if (e != cudaSuccess) return cuda_fail(e);
+    g_ws_ptr[dev] = p;
+    g_ws_bytes[dev] = need;
+  }
+  *out = g_ws_ptr[dev];
+  return KMX_OK;
+}
+
 }  // namespace
 
 DeviceInfo device_info(int dev) {
@@ -112,7 +139,11 @@ cudaError_t ensure_smem(const void* func, int dev, size_t bytes) {
 // Common driver: validated Problem -> launcher of the requested form.
 // ---------------------------------------------------------------------------
 static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream_t s) {
-  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  if (o.accumulate != KMX_ACC_ATOMIC && o.accumulate != KMX_ACC_DETERMINISTIC)
+    return KMX_ERR_INVALID_ARG;
+  // Deterministic mode groups entries by Y block.  The contiguous batched
+  // layout has one contribution per Y block and is deterministic already.
+  const bool det = o.accumulate == KMX_ACC_DETERMINISTIC && p.layout != L_BATCHED;
   // The generic kernel keeps one fiber of a square middle mode in a local
   // array of GEN_MAXN elements; larger n has no code path.
   const bool spec_n = (p.n[0] >= 2 && p.n[0] <= 8) || p.n[0] == 16;
@@ -122,12 +153,36 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   }
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
+  if (det) {
+    if (!is_square(p) || !spec_n || p.d < 3) return KMX_ERR_UNSUPPORTED;
+    const size_t need = seg_workspace_bytes(p.count);
+    void* ws = o.workspace;
+    size_t wsb = o.workspace_bytes;
+    if (ws == nullptr) {
+      rc = cached_workspace(need, s, &ws);
+      if (rc != KMX_OK) return rc;
+      wsb = need;
+    } else if (wsb < need) {
+      return KMX_ERR_WORKSPACE;
+    }
+    SegArrays sa;
+    cudaError_t se = seg_prepare(reinterpret_cast<void* const*>(p.Y), p.count,
+                                 p.Ny * (is_f64 ? 8 : 4), ws, wsb, p.status, s, &sa);
+    if (se != cudaSuccess) return cuda_fail(se);
+    p.seg_entries = sa.entries;
+    p.seg_offset = sa.offset;
+    p.seg_count = sa.count;
+    p.seg_order = sa.order;
+    p.seg_num = sa.num;
+    p.seg_queue = sa.queue;
+    p.y_exclusive = 1;  // a segment's Y block belongs to one group
+  }
   LaunchHint h = {0, 0, 0, 0};
   static const int engine_env = [] {
     const char* e = std::getenv("KMX_ENGINE");
     return e ? std::atoi(e) : 0;
   }();
-  h.engine = engine_env;
+  h.engine = o.engine ? o.engine : engine_env;
   cudaError_t e;
   if (!is_f64) {
     e = launch_f32_plain(p, h, s);
@@ -328,6 +383,11 @@ int kmx_kronmult_batched_f32(int d, int n, const float* A, float* X, float* Y, f
   return batched_impl<float>(d, n, A, X, Y, W, batchCount, nullptr, KMX_STREAM(stream));
 }
 
+int kmx_kronmult_batched_f32_ex(int d, int n, const float* A, float* X, float* Y, float* W,
+                                int batchCount, const kmx_options* opt, kmx_stream_t stream) {
+  return batched_impl<float>(d, n, A, X, Y, W, batchCount, opt, KMX_STREAM(stream));
+}
+
 int kmx_kronmult_pbatched_f64(int d, int n, const double* A, double* const* pX, double* const* pY,
                               double* const* pW, int batchCount, kmx_stream_t stream) {
   return pbatched_impl<double>(d, n, A, pX, pY, pW, batchCount, nullptr, KMX_STREAM(stream));
@@ -340,6 +400,12 @@ int kmx_kronmult_pbatched_f64_ex(int d, int n, const double* A, double* const* p
 int kmx_kronmult_pbatched_f32(int d, int n, const float* A, float* const* pX, float* const* pY,
                               float* const* pW, int batchCount, kmx_stream_t stream) {
   return pbatched_impl<float>(d, n, A, pX, pY, pW, batchCount, nullptr, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_pbatched_f32_ex(int d, int n, const float* A, float* const* pX, float* const* pY,
+                                 float* const* pW, int batchCount, const kmx_options* opt,
+                                 kmx_stream_t stream) {
+  return pbatched_impl<float>(d, n, A, pX, pY, pW, batchCount, opt, KMX_STREAM(stream));
 }
 
 int kmx_kronmult_xbatched_f64(int d, int n, const double* const* Aarray, int lda,
@@ -362,6 +428,14 @@ int kmx_kronmult_xbatched_f32(int d, int n, const float* const* Aarray, int lda,
                               KMX_STREAM(stream));
 }
 
+int kmx_kronmult_xbatched_f32_ex(int d, int n, const float* const* Aarray, int lda,
+                                 float* const* pX, float* const* pY, float* const* pW,
+                                 int batchCount, int subbatchCount, const kmx_options* opt,
+                                 kmx_stream_t stream) {
+  return xbatched_impl<float>(d, n, Aarray, lda, pX, pY, pW, batchCount, subbatchCount, opt,
+                              KMX_STREAM(stream));
+}
+
 int kmx_kronmult_vbatched_f64(int d, const int* m, const int* n, const double* const* Aarray,
                               double* const* pX, double* const* pY, double* W,
                               size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream) {
@@ -380,6 +454,32 @@ int kmx_kronmult_vbatched_f32(int d, const int* m, const int* n, const float* co
                               int batchCount, kmx_stream_t stream) {
   return vbatched_impl<float>(d, m, n, Aarray, pX, pY, W, Wcapacity_bytes, batchCount, nullptr,
                               KMX_STREAM(stream));
+}
+
+int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float* const* Aarray,
+                                 float* const* pX, float* const* pY, float* W,
+                                 size_t Wcapacity_bytes, int batchCount, const kmx_options* opt,
+                                 kmx_stream_t stream) {
+  return vbatched_impl<float>(d, m, n, Aarray, pX, pY, W, Wcapacity_bytes, batchCount, opt,
+                              KMX_STREAM(stream));
+}
+
+size_t kmx_deterministic_workspace_bytes(int batchCount) {
+  return batchCount > 0 ? seg_workspace_bytes(batchCount) : 0;
+}
+
+int kmx_release_workspace(kmx_stream_t stream) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e);
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_ws_ptr[dev]) {
+    e = cudaFreeAsync(g_ws_ptr[dev], KMX_STREAM(stream));
+    g_ws_ptr[dev] = nullptr;
+    g_ws_bytes[dev] = 0;
+    if (e != cudaSuccess) return cuda_fail(e);
+  }
+  return KMX_OK;
 }
 
 void kmx_set_default_options(const kmx_options* opt) {

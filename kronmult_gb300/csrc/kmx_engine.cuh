@@ -45,7 +45,7 @@ constexpr int MAX_THREADS = 512;
 enum Layout : int { L_BATCHED = 0, L_PBATCHED = 1, L_XBATCHED = 2, L_VBATCHED = 3 };
 
 // Bits of the device status word.
-enum DevFlag : int { DF_NULL_PTR = 1, DF_WAIT_TIMEOUT = 2, DF_BAD_SHAPE = 4, DF_NONFINITE_SPLIT = 8 };
+enum DevFlag : int { DF_NULL_PTR = 1, DF_WAIT_TIMEOUT = 2, DF_BAD_SHAPE = 4, DF_NONFINITE_SPLIT = 8, DF_OVERLAP = 16 };
 
 // Everything a launch needs.  Shapes are those of the APPLIED operator:
 // mode l maps n[l] -> m[l]; with trans != 0 factor l is read transposed
@@ -75,6 +75,13 @@ struct Problem {
   void* Wbase;           // wmode 3
   long long w_stride;    // wmode 3: elements between slots
   int nslots;            // concurrent workspace slots (grid*E must not exceed it)
+  // deterministic mode: entries grouped into Y segments (device arrays)
+  const int* seg_entries;  // entry ids sorted by Y block, original order within a block
+  const int* seg_offset;   // first position of segment s in seg_entries
+  const int* seg_count;    // entries of segment s
+  const int* seg_order;    // processing order of segments (longest first)
+  const int* seg_num;      // number of segments (device scalar)
+  int* seg_queue;          // work-queue counter, zero at launch
 };
 
 // ---------------------------------------------------------------------------

@@ -94,40 +94,42 @@ struct TileKernel {
   int group_smem = 0;
 };
 
-template <typename T, int FORM, int NN, int D>
+template <typename T, int FORM, int NN, int D, bool SEG>
 TileKernel tile_entry() {
   using Pol = typename TilePol<T, FORM>::type;
   TileKernel k;
-  constexpr int bytes = tile::group_smem_bytes<Pol, NN, D>();
+  constexpr int bytes = tile::group_smem_bytes<Pol, NN, D, SEG>();
   if constexpr (bytes <= 227 * 1024) {
-    k.func = reinterpret_cast<const void*>(&tile::tile_kernel<Pol, NN, D>);
+    k.func = reinterpret_cast<const void*>(&tile::tile_kernel<Pol, NN, D, SEG>);
     k.group_threads = tile::group_threads(NN, D);
     k.group_smem = bytes;
   }
   return k;
 }
 
-template <typename T, int FORM, int NN>
+template <typename T, int FORM, int NN, bool SEG>
 TileKernel tile_for_d(int d) {
   switch (d) {
-    case 3: return tile_entry<T, FORM, NN, 3>();
-    case 4: return tile_entry<T, FORM, NN, 4>();
-    case 5: return tile_entry<T, FORM, NN, 5>();
-    case 6: return tile_entry<T, FORM, NN, 6>();
+    case 3: return tile_entry<T, FORM, NN, 3, SEG>();
+    case 4: return tile_entry<T, FORM, NN, 4, SEG>();
+    case 5: return tile_entry<T, FORM, NN, 5, SEG>();
+    case 6: return tile_entry<T, FORM, NN, 6, SEG>();
     default: return TileKernel();
   }
 }
 
-template <typename T, int FORM>
+// Register-tiled kernel for (nn, d); SEG selects the deterministic
+// segment-queue variant.  func == nullptr when none exists.
+template <typename T, int FORM, bool SEG = false>
 TileKernel pick_tile(int nn, int d) {
   switch (nn) {
-    case 2: return tile_for_d<T, FORM, 2>(d);
-    case 3: return tile_for_d<T, FORM, 3>(d);
-    case 4: return tile_for_d<T, FORM, 4>(d);
-    case 5: return tile_for_d<T, FORM, 5>(d);
-    case 6: return tile_for_d<T, FORM, 6>(d);
-    case 7: return tile_for_d<T, FORM, 7>(d);
-    case 8: return tile_for_d<T, FORM, 8>(d);
+    case 2: return tile_for_d<T, FORM, 2, SEG>(d);
+    case 3: return tile_for_d<T, FORM, 3, SEG>(d);
+    case 4: return tile_for_d<T, FORM, 4, SEG>(d);
+    case 5: return tile_for_d<T, FORM, 5, SEG>(d);
+    case 6: return tile_for_d<T, FORM, 6, SEG>(d);
+    case 7: return tile_for_d<T, FORM, 7, SEG>(d);
+    case 8: return tile_for_d<T, FORM, 8, SEG>(d);
     default: return TileKernel();
   }
 }
@@ -193,6 +195,12 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   const DeviceInfo di = device_info(dev);
   const bool square = is_square(p);
   const int nn = p.n[0];
+  if (p.seg_entries) {
+    // deterministic mode: register-tiled segment kernels only
+    const TileKernel tk = square ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
+    if (!tk.func) return cudaErrorNotSupported;
+    return launch_tile(p, tk, hint, stream);
+  }
   if (square && hint.engine != 1) {
     const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
     if (tk.func) return launch_tile(p, tk, hint, stream);

@@ -53,12 +53,14 @@ __host__ __device__ constexpr int tile_size(int NN, int D, int p) {
 }
 
 // threads per entry: one tile per thread in the first phase where possible
+// (at most 512), and at least one thread per factor entry (d*NN*NN)
+__host__ __device__ constexpr int round32(int x) { return (x + 31) / 32 * 32; }
 __host__ __device__ constexpr int group_threads(int NN, int D) {
-  return (ipow(NN, D) / tile_size(NN, D, 0) + 31) / 32 * 32 > 512
-             ? 512
-             : ((ipow(NN, D) / tile_size(NN, D, 0) + 31) / 32 * 32 < 32
-                    ? 32
-                    : (ipow(NN, D) / tile_size(NN, D, 0) + 31) / 32 * 32);
+  return round32(ipow(NN, D) / tile_size(NN, D, 0)) > 512
+             ? (round32(D * NN * NN) > 512 ? round32(D * NN * NN) : 512)
+             : (round32(ipow(NN, D) / tile_size(NN, D, 0)) < round32(D * NN * NN)
+                    ? round32(D * NN * NN)
+                    : round32(ipow(NN, D) / tile_size(NN, D, 0)));
 }
 
 // physical slot of logical element q in the shared intermediate
@@ -245,141 +247,428 @@ __device__ __forceinline__ void middle_phases(typename Pol::V* buf, const typena
   }
 }
 
-// Shared memory per group: [d*NN*NN factor entries of V][MAXD+2 ints][buffer].
-template <class Pol, int NN, int D>
-__host__ __device__ constexpr int group_smem_bytes() {
-  return ((MAXD * NN * NN * (int)sizeof(typename Pol::V) + (MAXD + 2) * 4 + 15) / 16) * 16 +
-         ((buffer_slots<NN, D>() * (int)sizeof(typename Pol::V) + 15) / 16) * 16;
+// ---------------------------------------------------------------------------
+// TMA bulk copies and mbarriers.  Every wait is bounded (about 2 s of
+// %globaltimer); a wait that runs out sets DF_WAIT_TIMEOUT and the group
+// returns.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+  return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// One contiguous global -> shared bulk copy completing on `bar`.
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait until the phase of parity `parity` completes; false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > 2000000000ull) return false;
+    __nanosleep(32);
+  }
 }
 
+// ---------------------------------------------------------------------------
+// Entry pointers, one at a time (the pipeline loads them ahead of use).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long entry_index(const Problem& p, long long e) {
+  return p.order ? (long long)p.order[e] : e + p.entry_offset;
+}
+template <typename T>
+__device__ __forceinline__ const T* x_ptr(const Problem& p, long long ent) {
+  return p.layout == L_BATCHED ? static_cast<const T*>(p.X) + ent * p.Nx
+                               : static_cast<T* const*>(p.X)[ent];
+}
+template <typename T>
+__device__ __forceinline__ T* y_ptr(const Problem& p, long long ent) {
+  return p.layout == L_BATCHED ? static_cast<T*>(p.Y) + ent * p.Ny
+                               : static_cast<T* const*>(p.Y)[ent];
+}
+template <typename T>
+__device__ __forceinline__ const T* a_ptr(const Problem& p, long long ent, int l) {
+  if (p.layout == L_BATCHED || p.layout == L_PBATCHED)
+    return static_cast<const T*>(p.A) + (ent * p.d + l) * (long long)p.n[0] * p.n[0];
+  return static_cast<const T* const*>(p.A)[ent * p.d + l];
+}
+
+// ---------------------------------------------------------------------------
+// Shared memory per group:
+//   [d*NN*NN factor entries of V]
+//   [2 x (MAXD+1) exponent ints][2 flag ints][stage-mode int][pad]   (by entry parity)
+//   [2 entry descriptors (long long id, int flags, pad)]
+//   [mbarrier]
+//   [X staging block: N x In]
+//   [intermediate: buffer_slots x V]
+//   [segment accumulator: N x Out]   (deterministic mode only)
+// ---------------------------------------------------------------------------
 template <class Pol, int NN, int D>
-__global__ void __launch_bounds__(group_threads(NN, D) < 256 ? 256 : group_threads(NN, D))
+__host__ __device__ constexpr int off_ints() {
+  return MAXD * NN * NN * (int)sizeof(typename Pol::V);
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_desc() {
+  return (off_ints<Pol, NN, D>() + (2 * (MAXD + 1) + 4) * 4 + 15) / 16 * 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_bars() {
+  return off_desc<Pol, NN, D>() + 2 * 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_stage() {
+  return off_bars<Pol, NN, D>() + 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int stage_bytes() {
+  return (ipow(NN, D) * (int)sizeof(typename Pol::In) + 15) / 16 * 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int buf_bytes() {
+  return (buffer_slots<NN, D>() * (int)sizeof(typename Pol::V) + 15) / 16 * 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int acc_bytes() {
+  return (ipow(NN, D) * (int)sizeof(typename Pol::Out) + 15) / 16 * 16;
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_buf() {
+  return off_stage<Pol, NN, D>() + stage_bytes<Pol, NN, D>();
+}
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_acc() {
+  return off_buf<Pol, NN, D>() + buf_bytes<Pol, NN, D>();
+}
+template <class Pol, int NN, int D, bool SEG>
+__host__ __device__ constexpr int group_smem_bytes() {
+  return off_acc<Pol, NN, D>() + (SEG ? acc_bytes<Pol, NN, D>() : 0);
+}
+
+enum : int { TF_NULL = 1, TF_TIMEOUT = 2 };
+enum : int { ED_VALID = 1, ED_FIRST = 2 };  // entry descriptor flags
+
+struct EntryDesc {
+  long long ent;
+  int flags;
+  int pad;
+};
+
+// CTA size of the tile kernels, and the CTAs per SM they are compiled for
+// (caps registers at 128 per thread for CTAs of <= 256 threads).
+__host__ __device__ constexpr int cta_threads(int NN, int D) {
+  return group_threads(NN, D) < 256 ? 256 : group_threads(NN, D);
+}
+__host__ __device__ constexpr int min_ctas(int NN, int D) { return cta_threads(NN, D) > 256 ? 1 : 2; }
+
+// Software-pipelined entry loop of one group.
+//
+// SEG == false: entries in grid-stride order, contributions added to Y with
+//   RED (FP64/FP32 atomic add in L2).
+// SEG == true (deterministic mode): the group pops Y segments -- the entries
+//   sharing one Y block, in their original order -- from a device work queue;
+//   contributions are summed in a shared accumulator in a fixed order and
+//   added to the Y block once, by plain loads and stores (the group owns it).
+//
+// While entry k is contracted, the X block of entry k+1 streams into the
+// staging block by TMA (issued once entry k's X is in registers) and entry
+// k+1's factor entries are loaded into registers.  Thread 0 runs the entry
+// stream and publishes descriptors through shared memory.
+template <class Pol, int NN, int D, bool SEG>
+__global__ void __launch_bounds__(cta_threads(NN, D), min_ctas(NN, D))
 tile_kernel(const Problem p) {
   using V = typename Pol::V;
   using In = typename Pol::In;
+  using Out = typename Pol::Out;
   constexpr int G = group_threads(NN, D);
   constexpr int NN2 = NN * NN;
   constexpr int N = ipow(NN, D);
-  constexpr int LP = num_phases(NN, D) - 1;  // the last phase
+  constexpr int LP = num_phases(NN, D) - 1;
   constexpr int T0 = tile_size(NN, D, 0);
   constexpr int NT0 = N / T0;
   constexpr int TL = tile_size(NN, D, LP);
   constexpr int NTL = N / TL;
   constexpr bool PAIR0 = phase_b(NN, D, 0) >= 0;
   constexpr bool PAIRL = phase_b(NN, D, LP) >= 0;
+  constexpr int a0 = phase_a(NN, D, 0);
+  constexpr int b0 = PAIR0 ? phase_b(NN, D, 0) : a0;
   constexpr int aL = phase_a(NN, D, LP);
   constexpr int bL = PAIRL ? phase_b(NN, D, LP) : aL;
+  constexpr bool ONE = NT0 <= G;
+  constexpr uint32_t XBYTES = (uint32_t)N * sizeof(In);
 
   extern __shared__ __align__(16) unsigned char smem[];
   const int E = p.groups_per_cta;
   const int g = threadIdx.x / G;
   const int lt = threadIdx.x - g * G;
   if (g >= E) return;
-  unsigned char* gbase = smem + (size_t)g * group_smem_bytes<Pol, NN, D>();
-  V* sA = reinterpret_cast<V*>(gbase);
-  int* sExp = reinterpret_cast<int*>(gbase + MAXD * NN2 * sizeof(V));
-  V* buf = reinterpret_cast<V*>(
-      gbase + ((MAXD * NN2 * (int)sizeof(V) + (MAXD + 2) * 4 + 15) / 16) * 16);
-  const bool excl = p.y_exclusive != 0;
-  if (lt < MAXD + 2) sExp[lt] = 0;
+  unsigned char* gb = smem + (size_t)g * group_smem_bytes<Pol, NN, D, SEG>();
+  V* sA = reinterpret_cast<V*>(gb);
+  int* sExp = reinterpret_cast<int*>(gb + off_ints<Pol, NN, D>());  // [2][MAXD+1]
+  int* sFlag = sExp + 2 * (MAXD + 1);                                 // [2]
+  int* sMode = sFlag + 2;                                             // [1]
+  EntryDesc* sDesc = reinterpret_cast<EntryDesc*>(gb + off_desc<Pol, NN, D>());  // [2]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(gb + off_bars<Pol, NN, D>());
+  In* stage = reinterpret_cast<In*>(gb + off_stage<Pol, NN, D>());
+  V* buf = reinterpret_cast<V*>(gb + off_buf<Pol, NN, D>());
+  Out* acc = reinterpret_cast<Out*>(gb + off_acc<Pol, NN, D>());
+
+  // ---- entry stream (thread 0 only) ----
+  const long long gstep = (long long)gridDim.x * E;
+  long long rr_e = (long long)blockIdx.x * E + g;  // SEG == false: grid-stride position
+  int seg_pos = 0, seg_cnt = 0, seg_off = 0;        // SEG == true: current segment
+  auto next_desc = [&](EntryDesc& dsc) {
+    dsc.flags = 0;
+    dsc.ent = 0;
+    if constexpr (SEG) {
+      if (seg_pos >= seg_cnt) {
+        const int s = atomicAdd(p.seg_queue, 1);
+        if (s >= *p.seg_num) return;
+        const int sid = p.seg_order[s];
+        seg_off = p.seg_offset[sid];
+        seg_cnt = p.seg_count[sid];
+        seg_pos = 0;
+        dsc.flags |= ED_FIRST;
+      }
+      dsc.ent = p.seg_entries[seg_off + seg_pos];
+      ++seg_pos;
+      dsc.flags |= ED_VALID;
+    } else {
+      if (rr_e >= p.count) return;
+      dsc.ent = entry_index(p, rr_e);
+      rr_e += gstep;
+      dsc.flags = ED_VALID | ED_FIRST;
+    }
+  };
+
+  if (lt < 2 * (MAXD + 1) + 4) sExp[lt] = 0;
+  if (lt == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    EntryDesc d0;
+    next_desc(d0);
+    sDesc[0] = d0;
+  }
+  group_sync(g, G);
+  if (!(sDesc[0].flags & ED_VALID)) return;  // nothing for this group (uniform)
+
+  // factor entry owned by this thread (one per thread: G >= D*NN*NN)
+  const bool fthr = lt < D * NN2;
+  const int al = fthr ? lt / NN2 : 0;
+  const int ar = fthr ? (lt - al * NN2) / NN : 0;
+  const int aj = fthr ? lt - al * NN2 - ar * NN : 0;
+  const int ald = p.ld[al];
+  auto fetch_factor = [&](const In* Ap) -> In {
+    return p.trans ? Ap[aj + (long long)ar * ald] : Ap[ar + (long long)aj * ald];
+  };
+  uint32_t uses = 0;  // thread 0: completed phases of the barrier
+  auto issue_x = [&](const In* xsrc) {
+    int mode = 0;
+    if (xsrc != nullptr && ((reinterpret_cast<uintptr_t>(xsrc) & 15) == 0) && (XBYTES % 16 == 0)) {
+      fence_proxy_async();
+      mbar_expect_tx(bar, XBYTES);
+      tma_load_1d(stage, xsrc, XBYTES, bar);
+      mode = 1;
+    }
+    sMode[0] = mode;
+  };
+
+  // ---- prologue: first entry's factor entry and scale, its X block ----
+  In af = In(0);
+  {
+    const long long ent = sDesc[0].ent;
+    if (fthr) {
+      const In* Ap = a_ptr<In>(p, ent, al);
+      if (Ap) {
+        af = fetch_factor(Ap);
+        if constexpr (Pol::SCALED) atomicMax(&sExp[al], exp_field(af));
+      } else {
+        atomicOr(&sFlag[0], TF_NULL);
+      }
+    }
+    if (lt == 0) issue_x(x_ptr<In>(p, ent));
+  }
   group_sync(g, G);
 
-  const long long step = (long long)gridDim.x * E;
-  for (long long e = (long long)blockIdx.x * E + g; e < p.count; e += step) {
-    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
-    EntryPtrs<In> en;
-    if (!resolve_entry<In>(p, entry, en)) {
-      if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+  for (int k = 0;; ++k) {
+    const int pb = k & 1;
+    const EntryDesc dk = sDesc[pb];
+    if (!(dk.flags & ED_VALID)) break;
+    int* ex_k = sExp + pb * (MAXD + 1);
+    int* ex_n = sExp + (pb ^ 1) * (MAXD + 1);
+    const long long ent = dk.ent;
+    In* yp = y_ptr<In>(p, ent);
+    const In* xnext = nullptr;
+    if (lt == 0) {
+      EntryDesc dn;
+      next_desc(dn);
+      sDesc[pb ^ 1] = dn;
+      if (dn.flags & ED_VALID) xnext = x_ptr<In>(p, dn.ent);
+    }
+    if (fthr) sA[lt] = Pol::make(af, Pol::SCALED ? ex_k[al] : 0);
+    if (lt <= MAXD) ex_n[lt] = 0;
+    if (lt == 0) {
+      sFlag[pb ^ 1] = 0;
+      if (sMode[0]) {
+        const bool ok = mbar_wait(bar, uses & 1);
+        ++uses;
+        if (!ok) atomicOr(&sFlag[pb], TF_TIMEOUT);
+      }
+      if (!yp || !x_ptr<In>(p, ent)) atomicOr(&sFlag[pb], TF_NULL);
+    }
+    group_sync(g, G);  // S1: X staged, factors in shared memory, next descriptor published
+    const int flags = sFlag[pb];
+    if (flags & TF_TIMEOUT) {
+      if (lt == 0) atomicOr(p.status, DF_WAIT_TIMEOUT);
+      return;
+    }
+    const EntryDesc dn = sDesc[pb ^ 1];
+    const bool has_next = (dn.flags & ED_VALID) != 0;
+    const bool first = (dk.flags & ED_FIRST) != 0;
+    const bool last = !has_next || (dn.flags & ED_FIRST);
+    const In* anext = (has_next && fthr) ? a_ptr<In>(p, dn.ent, al) : nullptr;
+
+    auto fetch_next_factor = [&]() {
+      if (fthr && has_next) {
+        if (anext) {
+          af = fetch_factor(anext);
+        } else {
+          atomicOr(&sFlag[pb ^ 1], TF_NULL);
+        }
+      }
+    };
+    auto reduce_next_scale = [&]() {
+      if constexpr (Pol::SCALED) {
+        if (fthr && has_next && anext) atomicMax(&ex_n[al], exp_field(af));
+      }
+    };
+    // Deterministic mode, an entry without a contribution: keep the
+    // segment accumulator consistent (start it at zero, flush it at the end).
+    auto seg_fixup = [&]() {
+      if constexpr (SEG) {
+        for (int u = lt; u < NTL; u += G) {
+          const int base = tile_base<NN, D, LP>(u);
+#pragma unroll
+          for (int t = 0; t < TL; ++t) {
+            const int q = base + tile_off<NN, D, LP>(t);
+            const Out a = first ? Out(0) : acc[q];
+            if (last) {
+              if (yp) yp[q] += a;
+            } else {
+              acc[q] = a;
+            }
+          }
+        }
+      }
+    };
+    if (flags & TF_NULL) {
+      if (lt == 0) {
+        atomicOr(p.status, DF_NULL_PTR);
+        if (has_next) issue_x(xnext);
+      }
+      seg_fixup();
+      fetch_next_factor();
+      reduce_next_scale();
+      group_sync(g, G);
       continue;
     }
-    // ---- factor entries and their scales ----
-    In af = In(0);
-    const bool has_a = lt < D * NN2;
-    int al = 0, aidx = 0;
-    if (has_a) {
-      al = lt / NN2;
-      const int r = lt - al * NN2, ar = r / NN, aj = r - ar * NN;
-      aidx = lt;
-      af = p.trans ? en.A[al][aj + (long long)ar * en.ld[al]] : en.A[al][ar + (long long)aj * en.ld[al]];
-    }
-    for (int i = lt + G; i < D * NN2; i += G) {
-      // more factor entries than threads (large NN): stage raw values
-      const int l = i / NN2, r = i - l * NN2, ar = r / NN, aj = r - ar * NN;
-      const In v = p.trans ? en.A[l][aj + (long long)ar * en.ld[l]] : en.A[l][ar + (long long)aj * en.ld[l]];
-      if constexpr (Pol::SCALED) atomicMax(&sExp[l], exp_field(v));
-      reinterpret_cast<In*>(buf)[i] = v;
-    }
-    // ---- first tile(s) of X; with one tile per thread they stay in registers ----
-    constexpr bool ONE = NT0 <= G;
+
+    // ---- X tile of phase 0 and the block scale ----
+    const In* xs = sMode[0] ? stage : x_ptr<In>(p, ent);
     In xv[ONE ? T0 : 1];
+    int ex = 0, escale = 0;
+    if constexpr (ONE) {
+      if (lt < NT0) {
+        const int base = tile_base<NN, D, 0>(lt);
+#pragma unroll
+        for (int t = 0; t < T0; ++t) xv[t] = xs[base + tile_off<NN, D, 0>(t)];
+      }
+    }
     if constexpr (Pol::SCALED) {
-      int ex = 0;
+      int exl = 0;
       if constexpr (ONE) {
         if (lt < NT0) {
 #pragma unroll
-          for (int t = 0; t < T0; ++t) {
-            xv[t] = __ldg(en.X + tile_base<NN, D, 0>(lt) + tile_off<NN, D, 0>(t));
-            ex = max(ex, exp_field(xv[t]));
-          }
+          for (int t = 0; t < T0; ++t) exl = max(exl, exp_field(xv[t]));
         }
       } else {
-        for (int i = lt; i < N; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
+        for (int i = lt; i < N; i += G) exl = max(exl, exp_field(xs[i]));
       }
-      ex = __reduce_max_sync(0xffffffffu, ex);
-      if ((lt & 31) == 0 && ex > 0) atomicMax(&sExp[MAXD], ex);
-      if (has_a) atomicMax(&sExp[al], exp_field(af));
-    } else if constexpr (ONE) {
-      if (lt < NT0) {
-#pragma unroll
-        for (int t = 0; t < T0; ++t) xv[t] = __ldg(en.X + tile_base<NN, D, 0>(lt) + tile_off<NN, D, 0>(t));
-      }
+      exl = __reduce_max_sync(0xffffffffu, exl);
+      if ((lt & 31) == 0 && exl > 0) atomicMax(&ex_k[MAXD], exl);
     }
-    group_sync(g, G);
-    int escale = 0, ex = 0;
+    if constexpr (Pol::SCALED || ONE) {
+      group_sync(g, G);  // S2: X tiles in registers (stage free), block scale final
+    }
+    if (ONE && lt == 0 && has_next) issue_x(xnext);
     if constexpr (Pol::SCALED) {
-      bool skip = false, nonfinite = sExp[MAXD] == 2047;
-      ex = sExp[MAXD];
+      ex = ex_k[MAXD];
       escale = ex - 1023;
+      bool skip = ex == 0, nonfinite = ex == 2047;
 #pragma unroll
       for (int l = 0; l < D; ++l) {
-        escale += sExp[l] - 1023;
-        nonfinite = nonfinite || sExp[l] == 2047;
-        skip = skip || sExp[l] == 0;
+        escale += ex_k[l] - 1023;
+        skip = skip || ex_k[l] == 0;
+        nonfinite = nonfinite || ex_k[l] == 2047;
       }
-      skip = skip || ex == 0;
       if (skip || nonfinite) {
-        group_sync(g, G);  // every thread has read sExp
-        if (lt < MAXD + 2) sExp[lt] = 0;
+        if (!ONE && lt == 0 && has_next) issue_x(xnext);
         if constexpr (sizeof(In) == 8) {
-          // Inf/NaN must propagate exactly as in FP64: evaluate this entry in
-          // plain FP64 on the same shared memory (an all-zero factor or X
-          // without Inf/NaN contributes exactly zero and is skipped).
+          // Inf/NaN propagate exactly as in FP64: plain FP64 on the same
+          // shared memory (an all-zero factor or X contributes exactly zero).
           if (nonfinite) {
-            sq_plain_entry<double, NN, false>(p, *reinterpret_cast<EntryPtrs<double>*>(&en),
-                                              reinterpret_cast<double*>(sA),
+            EntryPtrs<double> en;
+            resolve_entry<double>(p, ent, en);
+            sq_plain_entry<double, NN, false>(p, en, reinterpret_cast<double*>(sA),
                                               reinterpret_cast<double*>(buf), lt, G, g);
+            group_sync(g, G);
           }
         }
+        seg_fixup();
+        fetch_next_factor();
+        reduce_next_scale();
         group_sync(g, G);
         continue;
       }
     }
-    if (has_a) sA[aidx] = Pol::make(af, Pol::SCALED ? sExp[al] : 0);
-    for (int i = lt + G; i < D * NN2; i += G) {
-      const int l = i / NN2;
-      sA[i] = Pol::make(reinterpret_cast<In*>(buf)[i], Pol::SCALED ? sExp[l] : 0);
-    }
-    group_sync(g, G);  // sA ready; buf staging free; sExp read by all
-    if (lt < MAXD + 2) sExp[lt] = 0;  // for the next entry (read above, before the barrier)
 
-    // ---- phase 0: X (HBM) -> registers -> contract -> buf ----
+    // ---- phase 0: registers -> buf ----
     if constexpr (ONE) {
       if (lt < NT0) {
         V v[T0];
 #pragma unroll
         for (int t = 0; t < T0; ++t) v[t] = Pol::make(xv[t], ex);
-        contract_tile<Pol, NN, PAIR0>(v, sA + phase_a(NN, D, 0) * NN2,
-                                      sA + (PAIR0 ? phase_b(NN, D, 0) : 0) * NN2);
+        contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
         const int base = tile_base<NN, D, 0>(lt);
 #pragma unroll
         for (int t = 0; t < T0; ++t) buf[slot<NN>(base + tile_off<NN, D, 0>(t))] = v[t];
@@ -389,17 +678,17 @@ tile_kernel(const Problem p) {
         const int base = tile_base<NN, D, 0>(u);
         V v[T0];
 #pragma unroll
-        for (int t = 0; t < T0; ++t) v[t] = Pol::make(__ldg(en.X + base + tile_off<NN, D, 0>(t)), ex);
-        contract_tile<Pol, NN, PAIR0>(v, sA + phase_a(NN, D, 0) * NN2,
-                                      sA + (PAIR0 ? phase_b(NN, D, 0) : 0) * NN2);
+        for (int t = 0; t < T0; ++t) v[t] = Pol::make(xs[base + tile_off<NN, D, 0>(t)], ex);
+        contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
 #pragma unroll
         for (int t = 0; t < T0; ++t) buf[slot<NN>(base + tile_off<NN, D, 0>(t))] = v[t];
       }
     }
-    group_sync(g, G);
-    // ---- middle phases: buf -> buf ----
+    fetch_next_factor();
+    group_sync(g, G);  // S3: buf complete; the staging block is free
+    if (!ONE && lt == 0 && has_next) issue_x(xnext);
     middle_phases<Pol, NN, D, G, 1>(buf, sA, lt, g);
-    // ---- last phase: buf -> contract -> Y (HBM) ----
+    // ---- last phase: buf -> Y ----
     for (int u = lt; u < NTL; u += G) {
       const int base = tile_base<NN, D, LP>(u);
       V v[TL];
@@ -408,11 +697,22 @@ tile_kernel(const Problem p) {
       contract_tile<Pol, NN, PAIRL>(v, sA + aL * NN2, sA + bL * NN2);
 #pragma unroll
       for (int t = 0; t < TL; ++t) {
-        const auto y = Pol::finish(v[t], escale);
-        y_accumulate(en.Y + base + tile_off<NN, D, LP>(t), y, excl);
+        const int q = base + tile_off<NN, D, LP>(t);
+        const Out y = Pol::finish(v[t], escale);
+        if constexpr (SEG) {
+          const Out a = first ? y : acc[q] + y;
+          if (last) {
+            yp[q] += a;
+          } else {
+            acc[q] = a;
+          }
+        } else {
+          atomicAdd(yp + q, y);
+        }
       }
     }
-    group_sync(g, G);
+    reduce_next_scale();
+    group_sync(g, G);  // trailing: sA, buf reusable; next entry's scales final
   }
 }
 

@@ -303,14 +303,15 @@ def test_missing_workspace_for_large_entry(kmx):
 
 @pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (5, 3), (3, 5)])
 def test_split_form_extreme_magnitudes(kmx, oracle, d, n):
-    """Factors and X spanning 1e-200..1e200: the split form rescales every
-    entry by powers of two, so its FP32 carriers never overflow or flush."""
+    """Factors scaled by 1e-30..1e30 each and X by 1e-60..1e60 (products stay
+    inside FP64 but far outside FP32): the split form rescales every entry by
+    powers of two, so its FP32 carriers never overflow or flush."""
     rng = np.random.default_rng(21)
     N = n ** d
     batch = 4
     A = rng.standard_normal((batch, d, n, n))
-    A *= 10.0 ** rng.integers(-200, 200, (batch, d, 1, 1))
-    X = rng.standard_normal((batch, N)) * 10.0 ** rng.integers(-150, 150, (batch, 1))
+    A *= 10.0 ** rng.integers(-30, 31, (batch, d, 1, 1))
+    X = rng.standard_normal((batch, N)) * 10.0 ** rng.integers(-60, 61, (batch, 1))
     Yref = np.zeros_like(X)
     oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
     Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
@@ -339,3 +340,96 @@ def test_nonfinite_inputs_propagate_like_fp64(kmx, oracle, form):
     assert np.array_equal(np.isinf(y), np.isinf(Yref))
     fin = np.isfinite(Yref).all(axis=1)
     assert blockwise_rel_err(y[fin], Yref[fin]) <= F64_TOL
+
+
+# ---------------------------------------------------------------------------
+# deterministic (sorted-segment) accumulation
+# ---------------------------------------------------------------------------
+
+def _pool_case(seed, d, n, pool=48, nx=40, ny=25, ne=700, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    N = n ** d
+    Apool = (rng.standard_normal((d, pool, n, n)) / 2).astype(dtype)
+    Xpool = rng.standard_normal((nx, N)).astype(dtype)
+    Y0 = rng.standard_normal((ny, N)).astype(dtype)
+    y_idx = rng.geometric(0.15, ne) % ny
+    x_idx = rng.integers(0, nx, ne)
+    a_idx = rng.integers(0, pool, (ne, d))
+    return Apool, Xpool, Y0, y_idx, x_idx, a_idx
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (5, 3), (3, 6)])
+def test_deterministic_xbatched_vs_oracle_and_bitwise(kmx, oracle, form, d, n):
+    Apool, Xpool, Y0, y_idx, x_idx, a_idx = _pool_case(31 + d + n, d, n)
+    N = n ** d
+    ne = len(y_idx)
+    Yref = Y0.copy()
+    oracle.xbatched_idx(d, n, Apool, n, Apool.shape[1], Xpool, Yref, y_idx, x_idx, a_idx)
+    Ad, Xd = dev(Apool), dev(Xpool)
+    pool = Apool.shape[1]
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xd, x_idx * N)
+    outs = []
+    for _ in range(3):
+        Yd = dev(Y0)
+        pY = kmx.pointer_array(Yd, y_idx * N)
+        kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, ne, form=form, accumulate="deterministic")
+        outs.append(host(Yd))
+    check_status(kmx)
+    assert blockwise_rel_err(outs[0], Yref) <= F64_TOL
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+def test_deterministic_f32_xbatched(kmx, oracle):
+    d, n = 4, 8
+    Apool, Xpool, Y0, y_idx, x_idx, a_idx = _pool_case(5, d, n, dtype=np.float32)
+    N = n ** d
+    ne = len(y_idx)
+    Yref = Y0.astype(np.float64)
+    oracle.xbatched_idx(d, n, Apool.astype(np.float64), n, Apool.shape[1], Xpool.astype(np.float64),
+                        Yref, y_idx, x_idx, a_idx)
+    Ad, Xd = dev(Apool), dev(Xpool)
+    pool = Apool.shape[1]
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xd, x_idx * N)
+    outs = []
+    for _ in range(2):
+        Yd = dev(Y0)
+        kmx.kronmult_xbatched(d, n, pA, n, pX, kmx.pointer_array(Yd, y_idx * N), None, ne,
+                              dtype=torch.float32, accumulate="deterministic")
+        outs.append(host(Yd))
+    assert blockwise_rel_err(outs[0], Yref) <= 1e-5
+    assert np.array_equal(outs[0], outs[1])
+    check_status(kmx)
+
+
+def test_deterministic_partial_overlap_is_refused(kmx):
+    """Y blocks that overlap without coinciding cannot be owned by one group:
+    the call writes nothing and reports KMX_ERR_OVERLAP (status bit 16)."""
+    d, n, ne = 4, 4, 6
+    N = n ** d
+    A = torch.rand((ne * d * n * n,), dtype=torch.float64, device="cuda")
+    X = torch.rand((ne, N), dtype=torch.float64, device="cuda")
+    Y = torch.zeros(4 * N, dtype=torch.float64, device="cuda")
+    pA = kmx.pointer_array(A, [i * n * n for i in range(ne * d)])
+    pX = kmx.pointer_array(X, [b * N for b in range(ne)])
+    pY = kmx.pointer_array(Y, [0, 0, N // 2, N, N, 2 * N])
+    kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, ne, accumulate="deterministic")
+    torch.cuda.synchronize()
+    with pytest.raises(kmx.KmxError) as ei:
+        kmx.check_device_status()
+    assert "DEVICE" in str(ei.value)
+    assert not Y.any()
+
+
+def test_deterministic_unsupported_shape(kmx):
+    d, n, ne = 2, 4, 3
+    N = n ** d
+    A = torch.rand((ne * d * n * n,), dtype=torch.float64, device="cuda")
+    X = torch.rand((ne, N), dtype=torch.float64, device="cuda")
+    Y = torch.zeros(N, dtype=torch.float64, device="cuda")
+    with pytest.raises(kmx.KmxError, match="UNSUPPORTED"):
+        kmx.kronmult_xbatched(d, n, kmx.pointer_array(A, [i * n * n for i in range(ne * d)]), n,
+                              kmx.pointer_array(X, [b * N for b in range(ne)]),
+                              kmx.pointer_array(Y, [0] * ne), None, ne, accumulate="deterministic")
