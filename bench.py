@@ -263,12 +263,12 @@ def run_ours(args):
     pA, pX, pY = ptrs(Ad, Xd, Yd)
     stream = torch.cuda.current_stream()
 
-    def step(form, Y_ptrs=pY):
-        kmx.kronmult_xbatched(D, NN, pA, NN, pX, Y_ptrs, None, entries, form=form)
+    def step(form, Y_ptrs=pY, acc="atomic"):
+        kmx.kronmult_xbatched(D, NN, pA, NN, pX, Y_ptrs, None, entries, form=form, accumulate=acc)
 
-    def timed(form, K, W):
+    def timed(form, K, W, acc="atomic"):
         for _ in range(W):
-            step(form)
+            step(form, acc=acc)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -276,7 +276,7 @@ def run_ours(args):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(K):
-            step(form)
+            step(form, acc=acc)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / K
@@ -292,6 +292,9 @@ def run_ours(args):
         ms = timed("auto", args.steps, args.warmup)
     clocks = clk.summary()
     kmx.check_device_status()
+    # deterministic sorted-segment accumulation (sort + segment queue inside every call)
+    ms_det = timed("auto", args.steps, args.warmup, acc="deterministic")
+    kmx.check_device_status()
 
     # accuracy: chosen vs plain on a fresh Y, and both vs the oracle on a sample
     Yc = torch.zeros_like(Xd)
@@ -304,6 +307,15 @@ def run_ours(args):
     num = torch.linalg.vector_norm(Yc - Yp, dim=1)
     den = torch.linalg.vector_norm(Yp, dim=1).clamp_min(1e-300)
     err_vs_plain = float((num / den).max().item())
+    Yd1 = torch.zeros_like(Xd)
+    Yd2 = torch.zeros_like(Xd)
+    step("auto", ptrs(Ad, Xd, Yd1)[2], acc="deterministic")
+    step("auto", ptrs(Ad, Xd, Yd2)[2], acc="deterministic")
+    torch.cuda.synchronize()
+    det_bitwise = bool(torch.equal(Yd1, Yd2))
+    num = torch.linalg.vector_norm(Yd1 - Yp, dim=1)
+    err_det_vs_plain = float((num / den).max().item())
+    del Yd1, Yd2
 
     total_flops = entries * flops_per_entry() * world
     value = total_flops / (ms * 1e-3) / 1e9
@@ -400,9 +412,13 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (256 MiB X and Y pools), no flush",
                    "seed": SEED, "parallelism": f"entries sharded per GPU x{world}"},
         "plain": {"value": round(value_plain, 3), "unit": "GFLOP/s", "ms_per_step": round(ms_plain, 4)},
+        "deterministic": {"value": round(total_flops / (ms_det * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
+                          "ms_per_step": round(ms_det, 4), "bitwise_repeatable": det_bitwise,
+                          "rel_err_vs_plain_atomic": err_det_vs_plain,
+                          "note": "device sort by Y block + segment work queue, per call"},
         "rel_err_chosen_vs_plain": err_vs_plain,
         "roofline": roofline, "north_star_roofline": north,
-        "gpu_launches": args.steps, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
+        "gpu_launches": args.steps, "gpu_launches_deterministic_per_step": 8, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
     if dist:
