@@ -164,6 +164,18 @@ int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float*
 void kmx_set_default_options(const kmx_options* opt);
 void kmx_get_default_options(kmx_options* opt);
 
+/* Deterministic xbatched (FP64, automatic form) that allocates nothing, for
+ * callers that cannot allocate device memory.  No counterpart in the
+ * reference.  Its sort and segment scratch is a fixed 16 MiB array in the
+ * library's device image (per GPU, held until exit); batches whose scratch
+ * exceeds it return KMX_ERR_WORKSPACE before any launch.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress): make it before any stream
+ * capture.  All calls share the array, so calls overlapping on the GPU race.
+ * Shapes: square n = 2..8, d = 3..6 (entries that fit on chip). */
+int kmx_kronmult_xbatched_f64_noalloc(int d, int n, const double* const* Aarray, int lda,
+                                      double* const* pX, double* const* pY, int batchCount,
+                                      kmx_stream_t stream);
+
 /* Device workspace the deterministic mode needs for batchCount entries. */
 size_t kmx_deterministic_workspace_bytes(int batchCount);
 

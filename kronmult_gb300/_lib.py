@@ -75,6 +75,7 @@ _SIGS = {
     "kmx_last_cuda_error": [],
     "kmx_probe_fma_rate": [_i, C.POINTER(C.c_double)],
     "kmx_release_workspace": [_vp],
+    "kmx_kronmult_xbatched_f64_noalloc": [_i, _i, _vp, _i, _vp, _vp, _i, _vp],
     "kmx_set_default_options": [_optp],
     "kmx_get_default_options": [_optp],
 }
