@@ -157,6 +157,30 @@ int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float*
                                  kmx_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Mixed shapes in one call (no counterpart in the reference, whose        */
+/* vbatched takes one shape per call, kronmult_vbatched.hpp:19-248).       */
+/* ---------------------------------------------------------------------- */
+
+/* Instance i (0 <= i < count) has dims[2i] = d_i and dims[2i+1] = n_i (square
+ * n_i x n_i factors, leading dimension n_i), factors Aarray[a_off[i] + l] for
+ * l < d_i, and blocks pX[i], pY[i]; dims, Aarray, a_off, pX, pY are device
+ * arrays.  classes is a HOST array of nclasses (d, n) pairs (<= 64) covering
+ * every instance; instances of other shapes are skipped and flagged in the
+ * device status word.  Instances are grouped by class on the device and each
+ * class runs its tuned kernel, in the order of the class list, without a host
+ * synchronisation (the call can be captured in a CUDA graph after one warm-up
+ * call).  W (Wcapacity_bytes) is needed only by classes whose entries exceed
+ * on-chip memory (slots of 2*n^d elements). */
+int kmx_kronmult_mixed_f64(int count, const int* dims, const double* const* Aarray,
+                           const long long* a_off, double* const* pX, double* const* pY,
+                           double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,
+                           const kmx_options* opt, kmx_stream_t stream);
+int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarray,
+                           const long long* a_off, float* const* pX, float* const* pY, float* W,
+                           size_t Wcapacity_bytes, const int* classes, int nclasses,
+                           const kmx_options* opt, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Library state and diagnostics.                                          */
 /* ---------------------------------------------------------------------- */
 

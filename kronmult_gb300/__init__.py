@@ -22,7 +22,7 @@ from ._lib import KmxError, check, exported_symbols, lib, options  # noqa: F401
 __all__ = [
     "KmxError", "lib", "options", "kron_flops", "pointer_array", "check_device_status",
     "kronmult_batched", "kronmult_pbatched", "kronmult_xbatched", "kronmult_vbatched",
-    "set_default_form",
+    "set_default_form", "kronmult_mixed",
 ]
 
 
@@ -176,6 +176,26 @@ def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, bat
         rc = L.kmx_kronmult_vbatched_f32_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
                                             _addr(W), cap, b, _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_vbatched")
+
+
+def kronmult_mixed(dims, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes=None, *,
+                   dtype=None, form=None, transpose=False, engine=None, stream=None):
+    """Instances of mixed (d, n) in one call.  dims: int32 CUDA tensor (count, 2)
+    of (d, n); Aarray: factor addresses, instance i's at a_off[i] .. a_off[i]+d-1
+    (a_off int64 CUDA tensor); pX/pY: block addresses; classes: host list of
+    (d, n) pairs covering every instance (processed in this order)."""
+    t = _torch()
+    f64 = _is_f64(dtype if dtype is not None else t.float64)
+    count = int(dims.shape[0])
+    flat = [int(v) for c in classes for v in c]
+    cl = (C.c_int * len(flat))(*flat)
+    cap = Wcapacity_bytes if Wcapacity_bytes is not None else (
+        W.numel() * W.element_size() if W is not None else 0)
+    s = C.c_void_p(_stream(stream))
+    fn = lib().kmx_kronmult_mixed_f64 if f64 else lib().kmx_kronmult_mixed_f32
+    rc = fn(count, _addr(dims), _addr(Aarray), _addr(a_off), _addr(pX), _addr(pY), _addr(W), cap,
+            cl, len(classes), _opt(form if f64 else None, None, transpose, engine), s)
+    check(rc, "kmx_kronmult_mixed")
 
 
 # Reference names, one per d, reference argument order.

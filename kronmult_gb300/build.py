@@ -41,9 +41,24 @@ def _compile(src: str, flags: list[str]) -> str:
     return obj
 
 
+def write_tune_header() -> None:
+    """csrc/kmx_tune_table.h from the committed tuning table (rewritten only
+    when its content changes, so unchanged builds stay incremental)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from kronmult_gb300.tune import header_from_table
+
+    text = header_from_table()
+    path = os.path.join(CSRC, "kmx_tune_table.h")
+    old = open(path).read() if os.path.exists(path) else None
+    if old != text:
+        with open(path, "w") as f:
+            f.write(text)
+
+
 def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
     """Compile every translation unit and link the library; returns its path."""
     os.makedirs(OBJDIR, exist_ok=True)
+    write_tune_header()
     flags = list(extra_flags or [])
     if verbose:
         flags += ["-Xptxas", "-v"]

@@ -10,7 +10,9 @@
 #include "../../include/kronmult_gb300.h"
 #include "kmx_forms.h"
 #include "kmx_launch.cuh"
+#include "kmx_mixed.h"
 #include "kmx_segments.h"
+#include "kmx_tune_table.h"
 
 namespace kmx {
 
@@ -32,9 +34,11 @@ std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 
 kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
 
-// Library-owned deterministic-mode workspace, one per device, stream ordered.
-void* g_ws_ptr[MAX_DEVICES];
-size_t g_ws_bytes[MAX_DEVICES];
+// Library-owned workspaces, stream ordered, one per device and purpose
+// (0: deterministic segments, 1: mixed-shape grouping).
+constexpr int WS_SLOTS = 2;
+void* g_ws_ptr[WS_SLOTS][MAX_DEVICES];
+size_t g_ws_bytes[WS_SLOTS][MAX_DEVICES];
 bool g_default_init = false;
 
 void init_defaults_locked() {
@@ -86,25 +90,25 @@ bool ipow_checked(int n, int d, long long* out) {
   return true;
 }
 
-int cached_workspace(size_t need, cudaStream_t s, void** out) {
+int cached_workspace(int slot, size_t need, cudaStream_t s, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e);
   std::lock_guard<std::mutex> lk(g_mu);
-  if (g_ws_bytes[dev] < need) {
-    if (g_ws_ptr[dev]) {
-      e = cudaFreeAsync(g_ws_ptr[dev], s);
+  if (g_ws_bytes[slot][dev] < need) {
+    if (g_ws_ptr[slot][dev]) {
+      e = cudaFreeAsync(g_ws_ptr[slot][dev], s);
       if (e != cudaSuccess) return cuda_fail(e);
-      g_ws_ptr[dev] = nullptr;
-      g_ws_bytes[dev] = 0;
+      g_ws_ptr[slot][dev] = nullptr;
+      g_ws_bytes[slot][dev] = 0;
     }
     void* p = nullptr;
     e = cudaMallocAsync(&p, need, s);
     if (e != cudaSuccess) return cuda_fail(e);
-    g_ws_ptr[dev] = p;
-    g_ws_bytes[dev] = need;
+    g_ws_ptr[slot][dev] = p;
+    g_ws_bytes[slot][dev] = need;
   }
-  *out = g_ws_ptr[dev];
+  *out = g_ws_ptr[slot][dev];
   return KMX_OK;
 }
 
@@ -135,6 +139,21 @@ cudaError_t ensure_smem(const void* func, int dev, size_t bytes) {
   return e;
 }
 
+// Tuned engine for (form code, d, n): 0 when the table has no row.
+static int tuned_engine(int form, int d, int n) {
+  for (int i = 0; i < kTuneRows; ++i)
+    if (kTuneTable[i].form == form && kTuneTable[i].d == d && kTuneTable[i].n == n)
+      return kTuneTable[i].engine;
+  return 0;
+}
+
+// Tuned automatic FP64 form for (d, n): 0 when the table has no row.
+static int tuned_form(int d, int n) {
+  for (int i = 0; i < kAutoRows; ++i)
+    if (kAutoTable[i].d == d && kAutoTable[i].n == n) return kAutoTable[i].form;
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // Common driver: validated Problem -> launcher of the requested form.
 // ---------------------------------------------------------------------------
@@ -159,7 +178,7 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     void* ws = o.workspace;
     size_t wsb = o.workspace_bytes;
     if (ws == nullptr) {
-      rc = cached_workspace(need, s, &ws);
+      rc = cached_workspace(0, need, s, &ws);
       if (rc != KMX_OK) return rc;
       wsb = need;
     } else if (wsb < need) {
@@ -184,13 +203,17 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   }();
   h.engine = o.engine ? o.engine : engine_env;
   cudaError_t e;
+  const bool sq = is_square(p);
   if (!is_f64) {
+    if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
     e = launch_f32_plain(p, h, s);
   } else {
     int form = o.form;
     if (form == KMX_FORM_AUTO) {
-      form = (is_square(p) && spec_n) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN;
+      const int t = sq ? tuned_form(p.d, p.n[0]) : 0;
+      form = t ? t : ((sq && spec_n) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
     }
+    if (h.engine == 0 && sq) h.engine = tuned_engine(form == KMX_FORM_SPLIT ? 2 : 1, p.d, p.n[0]);
     if (form == KMX_FORM_SPLIT) {
       e = launch_f64_split(p, h, s);
       if (e == cudaErrorNotSupported) e = launch_f64_plain(p, h, s);
@@ -362,6 +385,64 @@ static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarr
   return run_problem(p, sizeof(T) == 8, o, s);
 }
 
+// One call over instances of mixed (d, n): group by class on the device,
+// then one tuned launch per class reading its range from device memory.
+template <typename T>
+static int mixed_impl(int count, const int* dims, const T* const* Aarray, const long long* a_off,
+                      T* const* pX, T* const* pY, T* W, size_t Wcap, const int* classes,
+                      int nclasses, const kmx_options* opt, cudaStream_t s) {
+  if (count < 0 || nclasses < 1 || nclasses > KMX_MAX_CLASSES || !classes)
+    return KMX_ERR_INVALID_ARG;
+  if (count == 0) return KMX_OK;
+  if (!dims || !Aarray || !a_off || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  for (int c = 0; c < nclasses; ++c) {
+    const int d = classes[2 * c], n = classes[2 * c + 1];
+    long long N;
+    if (d < 1 || d > MAXD || n < 1) return KMX_ERR_INVALID_ARG;
+    if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  }
+  kmx_options o = resolve_options(opt);
+  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  int* status = nullptr;
+  int rc = status_ptr(&status);
+  if (rc != KMX_OK) return rc;
+  void* ws = nullptr;
+  const size_t need = mixed_workspace_bytes(count);
+  rc = cached_workspace(1, need, s, &ws);
+  if (rc != KMX_OK) return rc;
+  MixedArrays ma;
+  cudaError_t e = mixed_prepare(count, dims, classes, nclasses, ws, need, status, s, &ma);
+  if (e != cudaSuccess) return cuda_fail(e);
+  for (int c = 0; c < nclasses; ++c) {
+    const int d = classes[2 * c], n = classes[2 * c + 1];
+    long long N;
+    ipow_checked(n, d, &N);
+    Problem p;
+    base_square(p, L_MIXED, d, n, n, N);
+    p.count = count;  // upper bound for the grid; the kernels read the class count
+    p.count_dev = ma.counts + c;
+    p.order = ma.order;
+    p.order_base = ma.offsets + c;
+    p.a_off = a_off;
+    p.A = Aarray;
+    p.X = pX;
+    p.Y = const_cast<T**>(pY);
+    p.trans = o.transpose;
+    if (W && Wcap > 0) {
+      const size_t slot_bytes = 2 * (size_t)N * sizeof(T);
+      p.wmode = 3;
+      p.Wbase = W;
+      p.w_stride = 2 * N;
+      p.sxw = N;
+      const size_t slots = Wcap / slot_bytes;
+      p.nslots = (int)(slots < (size_t)count ? slots : (size_t)count);
+    }
+    rc = run_problem(p, sizeof(T) == 8, o, s);
+    if (rc != KMX_OK) return rc;
+  }
+  return KMX_OK;
+}
+
 }  // namespace kmx
 
 using namespace kmx;
@@ -464,6 +545,22 @@ int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float*
                               KMX_STREAM(stream));
 }
 
+int kmx_kronmult_mixed_f64(int count, const int* dims, const double* const* Aarray,
+                           const long long* a_off, double* const* pX, double* const* pY,
+                           double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,
+                           const kmx_options* opt, kmx_stream_t stream) {
+  return mixed_impl<double>(count, dims, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
+                            nclasses, opt, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarray,
+                           const long long* a_off, float* const* pX, float* const* pY, float* W,
+                           size_t Wcapacity_bytes, const int* classes, int nclasses,
+                           const kmx_options* opt, kmx_stream_t stream) {
+  return mixed_impl<float>(count, dims, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
+                           nclasses, opt, KMX_STREAM(stream));
+}
+
 size_t kmx_deterministic_workspace_bytes(int batchCount) {
   return batchCount > 0 ? seg_workspace_bytes(batchCount) : 0;
 }
@@ -473,11 +570,13 @@ int kmx_release_workspace(kmx_stream_t stream) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e);
   std::lock_guard<std::mutex> lk(g_mu);
-  if (g_ws_ptr[dev]) {
-    e = cudaFreeAsync(g_ws_ptr[dev], KMX_STREAM(stream));
-    g_ws_ptr[dev] = nullptr;
-    g_ws_bytes[dev] = 0;
-    if (e != cudaSuccess) return cuda_fail(e);
+  for (int slot = 0; slot < WS_SLOTS; ++slot) {
+    if (g_ws_ptr[slot][dev]) {
+      e = cudaFreeAsync(g_ws_ptr[slot][dev], KMX_STREAM(stream));
+      g_ws_ptr[slot][dev] = nullptr;
+      g_ws_bytes[slot][dev] = 0;
+      if (e != cudaSuccess) return cuda_fail(e);
+    }
   }
   return KMX_OK;
 }

@@ -42,7 +42,7 @@ namespace kmx {
 constexpr int MAXD = 6;
 constexpr int MAX_THREADS = 512;
 
-enum Layout : int { L_BATCHED = 0, L_PBATCHED = 1, L_XBATCHED = 2, L_VBATCHED = 3 };
+enum Layout : int { L_BATCHED = 0, L_PBATCHED = 1, L_XBATCHED = 2, L_VBATCHED = 3, L_MIXED = 4 };
 
 // Bits of the device status word.
 enum DevFlag : int { DF_NULL_PTR = 1, DF_WAIT_TIMEOUT = 2, DF_BAD_SHAPE = 4, DF_NONFINITE_SPLIT = 8, DF_OVERLAP = 16 };
@@ -82,7 +82,16 @@ struct Problem {
   const int* seg_order;    // processing order of segments (longest first)
   const int* seg_num;      // number of segments (device scalar)
   int* seg_queue;          // work-queue counter, zero at launch
+  // mixed-shape batches: this launch covers order[*order_base .. *order_base + *count_dev)
+  const long long* a_off;  // L_MIXED: first factor pointer of instance i in A
+  const int* count_dev;    // when set, the entry count is read from device memory
+  const int* order_base;   // when set, offset of this launch's entries in order[]
 };
+
+// Entries of a launch (device-side count when the host does not know it).
+__device__ __forceinline__ long long launch_count(const Problem& p) {
+  return p.count_dev ? (long long)*p.count_dev : (long long)p.count;
+}
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -145,7 +154,7 @@ __device__ __forceinline__ bool resolve_entry(const Problem& p, long long e, Ent
   } else {
     en.X = static_cast<T* const*>(p.X)[e];
     en.Y = static_cast<T* const*>(p.Y)[e];
-    const T* const* Ap = static_cast<const T* const*>(p.A) + e * d;
+    const T* const* Ap = static_cast<const T* const*>(p.A) + (p.a_off ? p.a_off[e] : e * d);
 #pragma unroll
     for (int l = 0; l < MAXD; ++l) {
       if (l < d) {
@@ -417,8 +426,10 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) 
   T* sbuf = sA + ((MAXD * NN2 * sizeof(T) + 15) / 16 * 16) / sizeof(T);
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
-  for (long long e = slot0; e < p.count; e += step) {
-    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+  const long long count = launch_count(p);
+  const long long obase = p.order_base ? (long long)*p.order_base : 0;
+  for (long long e = slot0; e < count; e += step) {
+    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
     EntryPtrs<T> en;
     if (!resolve_entry<T>(p, entry, en)) {
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
@@ -462,8 +473,10 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) 
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
   const bool excl = p.y_exclusive != 0;
-  for (long long e = slot0; e < p.count; e += step) {
-    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+  const long long count = launch_count(p);
+  const long long obase = p.order_base ? (long long)*p.order_base : 0;
+  for (long long e = slot0; e < count; e += step) {
+    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
     EntryPtrs<double> en;
     if (!resolve_entry<double>(p, entry, en)) {
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
@@ -624,8 +637,10 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
   const bool excl = p.y_exclusive != 0;
-  for (long long e = slot0; e < p.count; e += step) {
-    const long long entry = p.order ? (long long)p.order[e] : e + p.entry_offset;
+  const long long count = launch_count(p);
+  const long long obase = p.order_base ? (long long)*p.order_base : 0;
+  for (long long e = slot0; e < count; e += step) {
+    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
     EntryPtrs<T> en;
     if (!resolve_entry<T>(p, entry, en)) {
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);

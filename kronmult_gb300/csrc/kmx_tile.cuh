@@ -305,7 +305,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 // Entry pointers, one at a time (the pipeline loads them ahead of use).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ long long entry_index(const Problem& p, long long e) {
-  return p.order ? (long long)p.order[e] : e + p.entry_offset;
+  if (p.order) return (long long)p.order[(p.order_base ? (long long)*p.order_base : 0) + e];
+  return e + p.entry_offset;
 }
 template <typename T>
 __device__ __forceinline__ const T* x_ptr(const Problem& p, long long ent) {
@@ -321,7 +322,7 @@ template <typename T>
 __device__ __forceinline__ const T* a_ptr(const Problem& p, long long ent, int l) {
   if (p.layout == L_BATCHED || p.layout == L_PBATCHED)
     return static_cast<const T*>(p.A) + (ent * p.d + l) * (long long)p.n[0] * p.n[0];
-  return static_cast<const T* const*>(p.A)[ent * p.d + l];
+  return static_cast<const T* const*>(p.A)[(p.a_off ? p.a_off[ent] : ent * p.d) + l];
 }
 
 // ---------------------------------------------------------------------------
@@ -464,7 +465,7 @@ tile_kernel(const Problem p) {
       ++seg_pos;
       dsc.flags |= ED_VALID;
     } else {
-      if (rr_e >= p.count) return;
+      if (rr_e >= launch_count(p)) return;
       dsc.ent = entry_index(p, rr_e);
       rr_e += gstep;
       dsc.flags = ED_VALID | ED_FIRST;

@@ -433,3 +433,108 @@ def test_deterministic_unsupported_shape(kmx):
         kmx.kronmult_xbatched(d, n, kmx.pointer_array(A, [i * n * n for i in range(ne * d)]), n,
                               kmx.pointer_array(X, [b * N for b in range(ne)]),
                               kmx.pointer_array(Y, [0] * ne), None, ne, accumulate="deterministic")
+
+
+# ---------------------------------------------------------------------------
+# mixed shapes in one call, and CUDA-graph capture of repeated calls
+# ---------------------------------------------------------------------------
+
+def _mixed_case(kmx, seed, count, ns=(2, 3, 4, 5, 6, 8), dmax=6, cap=262144, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    dims = []
+    while len(dims) < count:
+        d = int(rng.integers(1, dmax + 1))
+        n = int(rng.choice(ns))
+        if n ** d <= cap:
+            dims.append((d, n))
+    dims = np.array(dims, dtype=np.int32)
+    factors, xs, ys, a_off = [], [], [], []
+    o = 0
+    for d, n in dims:
+        a_off.append(o)
+        for _ in range(d):
+            factors.append(rng.uniform(-1, 1, n * n).astype(dtype))
+            o += 1
+        xs.append(rng.uniform(-1, 1, n ** d).astype(dtype))
+        ys.append(rng.uniform(-1, 1, n ** d).astype(dtype))
+    # pack into flat device buffers
+    fbuf = dev(np.concatenate(factors))
+    foffs = np.cumsum([0] + [f.size for f in factors[:-1]])
+    xbuf, ybuf = dev(np.concatenate(xs)), dev(np.concatenate(ys))
+    xoffs = np.cumsum([0] + [x.size for x in xs[:-1]])
+    pA = kmx.pointer_array(fbuf, foffs)
+    pX = kmx.pointer_array(xbuf, xoffs)
+    classes = sorted({(int(d), int(n)) for d, n in dims}, key=lambda c: -(c[1] ** (c[0] + 1) * c[0]))
+    return dict(dims=dims, factors=factors, xs=xs, ys=ys, a_off=np.array(a_off), fbuf=fbuf,
+                xbuf=xbuf, ybuf=ybuf, xoffs=xoffs, pA=pA, pX=pX, classes=classes)
+
+
+def _mixed_reference(oracle, c):
+    out = []
+    fi = 0
+    for i, (d, n) in enumerate(c["dims"]):
+        fs = c["factors"][c["a_off"][i]: c["a_off"][i] + d]
+        y = c["ys"][i].astype(np.float64).copy()
+        oracle.kronmultv(int(d), [int(n)] * d, [int(n)] * d, [f.astype(np.float64) for f in fs],
+                         [int(n)] * d, c["xs"][i].astype(np.float64), y)
+        out.append(y)
+    return out
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_shapes_one_call(kmx, oracle, form):
+    c = _mixed_case(kmx, 41, 300)
+    ybuf = c["ybuf"].clone()
+    pY = kmx.pointer_array(ybuf, c["xoffs"])
+    W = torch.empty(4 * 2 * 8 ** 6, dtype=torch.float64, device="cuda")  # 4 slots for 8^6 entries
+    kmx.kronmult_mixed(dev(c["dims"]), c["pA"], dev(c["a_off"].astype(np.int64)), c["pX"], pY,
+                       c["classes"], W, form=form)
+    y = host(ybuf)
+    ref = _mixed_reference(oracle, c)
+    for i, r in enumerate(ref):
+        seg = y[c["xoffs"][i]: c["xoffs"][i] + r.size]
+        assert blockwise_rel_err(seg, r) <= F64_TOL, (i, c["dims"][i])
+    check_status(kmx)
+
+
+def test_mixed_unknown_class_is_flagged(kmx):
+    c = _mixed_case(kmx, 42, 20, ns=(2, 3), dmax=3)
+    ybuf = c["ybuf"].clone()
+    pY = kmx.pointer_array(ybuf, c["xoffs"])
+    kmx.kronmult_mixed(dev(c["dims"]), c["pA"], dev(c["a_off"].astype(np.int64)), c["pX"], pY,
+                       c["classes"][:-1])
+    torch.cuda.synchronize()
+    with pytest.raises(kmx.KmxError):
+        kmx.check_device_status()
+
+
+def test_cuda_graph_of_repeated_mixed_calls(kmx, oracle):
+    """A sequence of calls captured once as a CUDA graph and replayed gives the
+    same result as the eager calls (one warm-up call first)."""
+    c = _mixed_case(kmx, 43, 120, dmax=5)
+    dims_d, aoff_d = dev(c["dims"]), dev(c["a_off"].astype(np.int64))
+    reps = 10
+    y_eager = c["ybuf"].clone()
+    pY_e = kmx.pointer_array(y_eager, c["xoffs"])
+    y_graph = c["ybuf"].clone()
+    pY_g = kmx.pointer_array(y_graph, c["xoffs"])
+    W = torch.empty(2 * 8 ** 5 * 4, dtype=torch.float64, device="cuda")
+    # warm-up (caches workspaces and kernel attributes), then undo it
+    kmx.kronmult_mixed(dims_d, c["pA"], aoff_d, c["pX"], pY_g, c["classes"], W, form="split")
+    torch.cuda.synchronize()
+    y_graph.copy_(c["ybuf"])
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            for _ in range(reps):
+                kmx.kronmult_mixed(dims_d, c["pA"], aoff_d, c["pX"], pY_g, c["classes"], W,
+                                   form="split", stream=s)
+    torch.cuda.current_stream().wait_stream(s)
+    g.replay()
+    for _ in range(reps):
+        kmx.kronmult_mixed(dims_d, c["pA"], aoff_d, c["pX"], pY_e, c["classes"], W, form="split")
+    torch.cuda.synchronize()
+    assert blockwise_rel_err(host(y_graph), host(y_eager)) <= 1e-12
+    check_status(kmx)
