@@ -157,6 +157,27 @@ int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float*
                                  kmx_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Differentiation (no counterpart in the reference, which has no backward).  */
+/* ---------------------------------------------------------------------- */
+
+/* Fused forward + backward of the batched layout for loss = sum(G .* Y):
+ *   Y  += (A1 x ... x Ad) X          (when Y != NULL)
+ *   dX += (A1^T x ... x Ad^T) G      (when dX != NULL)
+ *   dA_k += sum over the other indices of B_k[.., a, ..] F_k[.., b, ..]  (when dA != NULL)
+ * with F_k = X contracted by A_l for l < k and B_k = G contracted by A_l^T for
+ * l > k, recomputed on chip.  A, dA are (n,n,d,batch) column-major; X, G, Y, dX
+ * are (n^d, batch).  Square n = 2..8.  W (Wcapacity_bytes) holds (d-1)*n^d
+ * elements per concurrent entry when the intermediates exceed shared memory
+ * (about 200 KB per entry); otherwise it may be NULL. */
+int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
+                                  const double* G, double* Y, double* dX, double* dA,
+                                  double* W, size_t Wcapacity_bytes, int batchCount,
+                                  kmx_stream_t stream);
+int kmx_kronmult_batched_grad_f32(int d, int n, const float* A, const float* X, const float* G,
+                                  float* Y, float* dX, float* dA, float* W,
+                                  size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Mixed shapes in one call (no counterpart in the reference, whose        */
 /* vbatched takes one shape per call, kronmult_vbatched.hpp:19-248).       */
 /* ---------------------------------------------------------------------- */

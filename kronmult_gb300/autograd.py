@@ -1,0 +1,81 @@
+"""torch.autograd.Function over the C ABI's forward and fused backward.
+
+Layout (the reference's batched layout, kronmult6_batched.hpp:14-94):
+  A: (batch, d, n, n) tensor whose [b, l] slice holds factor A_l of entry b in
+     COLUMN-major order, i.e. A[b, l, j, i] = A_l(i, j) (A[b, l].T is the matrix);
+  X: (batch, n**d); the result Y has the same shape.
+
+Forward runs the tuned forward kernel; backward runs the fused kernel that
+recomputes the forward intermediates on chip (nothing is stored between the
+two) and returns dA, dX.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib, kronmult_batched
+
+
+def _grad_call(d, n, A, X, G, Y, dX, dA, W):
+    L = _lib.lib()
+    f64 = A.dtype == torch.float64
+    fn = L.kmx_kronmult_batched_grad_f64 if f64 else L.kmx_kronmult_batched_grad_f32
+
+    def a(t):
+        return t.data_ptr() if t is not None else None
+
+    cap = W.numel() * W.element_size() if W is not None else 0
+    rc = fn(d, n, a(A), a(X), a(G), a(Y), a(dX), a(dA), a(W), cap, A.shape[0],
+            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "kmx_kronmult_batched_grad")
+
+
+def grad_workspace(d, n, batch, dtype=torch.float64, device="cuda"):
+    """Workspace for the fused backward when an entry's intermediates exceed
+    shared memory (one slot per concurrently processed entry)."""
+    N = n ** d
+    esz = 8 if dtype == torch.float64 else 4
+    if 2 * 6 * n * n * esz + N * esz * max(d, 1) <= 200 * 1024:
+        return None
+    slots = min(batch, 304)
+    return torch.empty(slots * max(d - 1, 1) * N, dtype=dtype, device=device)
+
+
+def kronmult_fused_grad(A, X, G, want_y=True):
+    """Y, dX, dA of loss = sum(G * Y) in one launch."""
+    batch, d, n, _ = A.shape
+    Y = torch.zeros_like(X) if want_y else None
+    dX = torch.zeros_like(X)
+    dA = torch.zeros_like(A)
+    _grad_call(d, n, A.contiguous(), X.contiguous(), G.contiguous(), Y, dX, dA,
+               grad_workspace(d, n, batch, A.dtype))
+    return Y, dX, dA
+
+
+class KronmultFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, A, X, form=None):
+        batch, d, n, _ = A.shape
+        A = A.contiguous()
+        X = X.contiguous()
+        Y = torch.zeros_like(X)
+        kronmult_batched(d, n, A, X, Y, None, batch, form=form)
+        ctx.save_for_backward(A, X)
+        return Y
+
+    @staticmethod
+    def backward(ctx, G):
+        A, X = ctx.saved_tensors
+        batch, d, n, _ = A.shape
+        need_a, need_x = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        dX = torch.zeros_like(X) if need_x else None
+        dA = torch.zeros_like(A) if need_a else None
+        _grad_call(d, n, A, X, G.contiguous(), None, dX, dA, grad_workspace(d, n, batch, A.dtype))
+        return dA, dX, None
+
+
+def kronmult(A, X, form=None):
+    """Differentiable Y = kron(A_1, ..., A_d) X per entry (see module doc)."""
+    return KronmultFunction.apply(A, X, form)

@@ -114,6 +114,8 @@ int cached_workspace(int slot, size_t need, cudaStream_t s, void** out) {
 
 }  // namespace
 
+int device_status_ptr(int** out) { return status_ptr(out); }
+
 DeviceInfo device_info(int dev) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (dev >= 0 && dev < MAX_DEVICES && g_dev_ok[dev]) return g_dev[dev];

@@ -1,0 +1,288 @@
+// kmx_grad.cu -- fused forward + backward of the batched Kronecker mat-vec.
+//
+// For one entry, with Y = (A_1 x ... x A_d) X and an upstream gradient G
+// (loss = sum G .* Y):
+//   F_k = X with modes l < k contracted by A_l        (forward intermediates)
+//   B_k = G with modes l > k contracted by A_l^T      (backward intermediates)
+//   dA_k(a, b) = sum over the other indices of B_k[.., a, ..] * F_k[.., b, ..]
+//   dX = A_1^T applied to B_1  ( = (A_1^T x ... x A_d^T) G )
+//   Y  = A_d applied to F_d
+// (0-based in the code: modes 0..d-1.)  The forward intermediates are
+// recomputed from X on chip -- a forward call stores nothing -- and kept in
+// shared memory when they fit, else in a per-group slot of the caller's
+// workspace.  The B sweep runs in place in shared memory; each Gram is
+// accumulated per thread in registers and reduced with shared-memory atomics.
+// Every output is accumulated into (Y +=, dX +=, dA +=) like Y in the forward
+// entry points.  Flops: 3d mode products versus d for the forward.
+#include <cuda_runtime.h>
+
+#include "../../include/kronmult_gb300.h"
+#include "kmx_engine.cuh"
+#include "kmx_launch.cuh"
+
+namespace kmx {
+
+struct GradProblem {
+  int d;
+  int N;
+  int batch;
+  const void* A;   // (n, n, d, batch) column-major
+  const void* X;   // (N, batch)
+  const void* G;   // (N, batch)
+  void* Y;         // (N, batch) or null
+  void* dX;        // (N, batch) or null
+  void* dA;        // (n, n, d, batch) or null
+  void* W;         // global slots for the forward intermediates (or null)
+  long long wslot; // elements per slot
+  int nslots;
+  int f_in_smem;   // forward intermediates in shared memory
+  int* status;
+};
+
+namespace {
+
+template <typename T, int NN>
+__device__ __forceinline__ void mode_apply(const T* src, T* dst, const T* A, bool transA, int s,
+                                           int F, int lt, int G) {
+  // dst[o, a, r] = sum_j A(a, j) src[o, j, r] along the mode of stride s; dst may equal src
+  const FastDiv fd((unsigned)s);
+  for (int f = lt; f < F; f += G) {
+    const unsigned o = fd((unsigned)f);
+    const int r0 = f - (int)o * s;
+    const long long base = (long long)o * NN * s + r0;
+    T v[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) v[j] = src[base + (long long)j * s];
+#pragma unroll
+    for (int a = 0; a < NN; ++a) {
+      // A(a, j) = A[a*NN + j]; its transpose reads A[j*NN + a]
+      T acc = (transA ? A[0 * NN + a] : A[a * NN + 0]) * v[0];
+#pragma unroll
+      for (int j = 1; j < NN; ++j) acc = fma(transA ? A[j * NN + a] : A[a * NN + j], v[j], acc);
+      dst[base + (long long)a * s] = acc;
+    }
+  }
+}
+
+// Gram along the mode of stride s: dA(a, b) += sum_fibers B[a] * Fk[b].
+template <typename T, int NN>
+__device__ __forceinline__ void mode_gram(const T* B, const T* Fk, T* sdA, int s, int F, int lt,
+                                          int G) {
+  constexpr int ROWS = NN <= 5 ? NN : 2;
+  const FastDiv fd((unsigned)s);
+  for (int r0 = 0; r0 < NN; r0 += ROWS) {
+    T acc[ROWS][NN];
+#pragma unroll
+    for (int a = 0; a < ROWS; ++a)
+#pragma unroll
+      for (int b = 0; b < NN; ++b) acc[a][b] = T(0);
+    for (int f = lt; f < F; f += G) {
+      const unsigned o = fd((unsigned)f);
+      const int r = f - (int)o * s;
+      const long long base = (long long)o * NN * s + r;
+      T x[NN];
+#pragma unroll
+      for (int b = 0; b < NN; ++b) x[b] = Fk[base + (long long)b * s];
+#pragma unroll
+      for (int a = 0; a < ROWS; ++a) {
+        if (r0 + a < NN) {
+          const T bv = B[base + (long long)(r0 + a) * s];
+#pragma unroll
+          for (int b = 0; b < NN; ++b) acc[a][b] = fma(bv, x[b], acc[a][b]);
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < ROWS; ++a)
+      if (r0 + a < NN)
+#pragma unroll
+        for (int b = 0; b < NN; ++b) atomicAdd(&sdA[(r0 + a) * NN + b], acc[a][b]);
+  }
+}
+
+// sA holds A_l row-major: sA[l*NN*NN + a*NN + j] = A_l(a, j).
+template <typename T, int NN>
+__global__ void __launch_bounds__(256) grad_kernel(const GradProblem gp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NN2 = NN * NN;
+  const int d = gp.d, N = gp.N, F = N / NN;
+  const int lt = threadIdx.x, G = blockDim.x;
+  T* sA = reinterpret_cast<T*>(smem);
+  T* sdA = sA + MAXD * NN2;
+  T* sB = sdA + MAXD * NN2;
+  T* sF = sB + N;  // (d-1) forward intermediates when they fit
+  const long long slot = blockIdx.x;
+  T* Fst = gp.f_in_smem ? sF
+                        : (gp.W ? static_cast<T*>(gp.W) + slot * gp.wslot : nullptr);
+  if (Fst == nullptr) {
+    if (lt == 0) atomicOr(gp.status, DF_NULL_PTR);
+    return;
+  }
+  for (long long e = blockIdx.x; e < gp.batch; e += gridDim.x) {
+    const T* Ae = static_cast<const T*>(gp.A) + e * d * NN2;
+    for (int i = lt; i < d * NN2; i += G) {
+      const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
+      sA[i] = Ae[l * NN2 + a + j * NN];
+      sdA[i] = T(0);
+    }
+    __syncthreads();
+    const T* Xe = static_cast<const T*>(gp.X) + e * N;
+    const T* Ge = static_cast<const T*>(gp.G) + e * N;
+    // forward sweep: F_{k+1} = mode k of F_k, F_0 = X
+    int s = N / NN;
+    for (int k = 0; k < d - 1; ++k, s /= NN) {
+      const T* src = k == 0 ? Xe : Fst + (long long)(k - 1) * N;
+      mode_apply<T, NN>(src, Fst + (long long)k * N, sA + k * NN2, false, s, F, lt, G);
+      __syncthreads();
+    }
+    // forward output (s is now 1: the last mode)
+    if (gp.Y) {
+      T* Ye = static_cast<T*>(gp.Y) + e * N;
+      const T* src = d == 1 ? Xe : Fst + (long long)(d - 2) * N;
+      const T* Ad = sA + (d - 1) * NN2;
+      for (int i = lt; i < N; i += G) {
+        const int f = i / NN, a = i - f * NN;
+        T acc = Ad[a * NN] * src[(long long)f * NN];
+#pragma unroll
+        for (int j = 1; j < NN; ++j) acc = fma(Ad[a * NN + j], src[(long long)f * NN + j], acc);
+        Ye[i] += acc;
+      }
+    }
+    // backward sweep from B = G
+    for (int i = lt; i < N; i += G) sB[i] = Ge[i];
+    __syncthreads();
+    s = 1;
+    for (int k = d - 1; k >= 0; --k, s *= NN) {
+      const T* Fk = k == 0 ? Xe : Fst + (long long)(k - 1) * N;
+      if (gp.dA) mode_gram<T, NN>(sB, Fk, sdA + k * NN2, s, F, lt, G);
+      if (k > 0) {
+        __syncthreads();  // the Gram read sB before it is overwritten
+        mode_apply<T, NN>(sB, sB, sA + k * NN2, true, s, F, lt, G);
+        __syncthreads();
+      } else if (gp.dX) {
+        T* dXe = static_cast<T*>(gp.dX) + e * N;
+        // dX += A_0^T along mode 0 (stride N / NN), one output per thread
+        const FastDiv fd((unsigned)s);
+        for (int f = lt; f < F; f += G) {
+          const unsigned o = fd((unsigned)f);
+          const int r0 = f - (int)o * s;
+          const long long base = (long long)o * NN * s + r0;
+          T v[NN];
+#pragma unroll
+          for (int j = 0; j < NN; ++j) v[j] = sB[base + (long long)j * s];
+#pragma unroll
+          for (int a = 0; a < NN; ++a) {
+            T acc = sA[0 * NN + a] * v[0];
+#pragma unroll
+            for (int j = 1; j < NN; ++j) acc = fma(sA[j * NN + a], v[j], acc);
+            dXe[base + (long long)a * s] += acc;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (gp.dA) {
+      T* dAe = static_cast<T*>(gp.dA) + e * d * NN2;
+      for (int i = lt; i < d * NN2; i += G) {
+        const int l = i / NN2, r = i - l * NN2, a = r / NN, b = r - a * NN;
+        dAe[l * NN2 + a + b * NN] += sdA[i];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int NN>
+const void* grad_func() {
+  return reinterpret_cast<const void*>(&grad_kernel<T, NN>);
+}
+
+template <typename T>
+const void* pick_grad(int n) {
+  switch (n) {
+    case 2: return grad_func<T, 2>();
+    case 3: return grad_func<T, 3>();
+    case 4: return grad_func<T, 4>();
+    case 5: return grad_func<T, 5>();
+    case 6: return grad_func<T, 6>();
+    case 7: return grad_func<T, 7>();
+    case 8: return grad_func<T, 8>();
+    default: return nullptr;
+  }
+}
+
+template <typename T>
+int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* dA, T* W,
+              size_t Wbytes, int batch, cudaStream_t s) {
+  if (d < 1 || d > MAXD || n < 1 || batch < 0) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!A || !X || !G) return KMX_ERR_NULL_POINTER;
+  const void* func = pick_grad<T>(n);
+  if (!func) return KMX_ERR_UNSUPPORTED;
+  long long N = 1;
+  for (int i = 0; i < d; ++i) N *= n;
+  if (N > (1LL << 28)) return KMX_ERR_UNSUPPORTED;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return KMX_ERR_CUDA;
+  const DeviceInfo di = device_info(dev);
+  GradProblem gp;
+  gp.d = d;
+  gp.N = (int)N;
+  gp.batch = batch;
+  gp.A = A;
+  gp.X = X;
+  gp.G = G;
+  gp.Y = Y;
+  gp.dX = dX;
+  gp.dA = dA;
+  gp.W = W;
+  gp.wslot = (long long)(d > 1 ? d - 1 : 1) * N;
+  const size_t head = 2 * (size_t)MAXD * n * n * sizeof(T);
+  const size_t with_f = head + (size_t)N * sizeof(T) * (d > 1 ? d : 1);
+  const size_t without_f = head + (size_t)N * sizeof(T);
+  size_t smem;
+  if (with_f <= 200 * 1024) {
+    gp.f_in_smem = 1;
+    smem = with_f;
+    gp.nslots = batch;
+  } else {
+    if (without_f > (size_t)di.max_smem_optin) return KMX_ERR_UNSUPPORTED;
+    gp.f_in_smem = 0;
+    smem = without_f;
+    const size_t slot_bytes = (size_t)gp.wslot * sizeof(T);
+    gp.nslots = W ? (int)(Wbytes / slot_bytes < (size_t)batch ? Wbytes / slot_bytes : batch) : 0;
+    if (gp.nslots < 1) return KMX_ERR_WORKSPACE;
+  }
+  int rc = device_status_ptr(&gp.status);
+  if (rc != KMX_OK) return rc;
+  cudaError_t e = ensure_smem(func, dev, smem);
+  if (e != cudaSuccess) return KMX_ERR_CUDA;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, 256, smem);
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)di.sms * per_sm;
+  if (grid > batch) grid = batch;
+  if (!gp.f_in_smem && grid > gp.nslots) grid = gp.nslots;
+  void* args[] = {&gp};
+  e = cudaLaunchKernel(func, dim3((unsigned)grid), dim3(256), args, smem, s);
+  return e == cudaSuccess ? KMX_OK : KMX_ERR_CUDA;
+}
+
+}  // namespace
+}  // namespace kmx
+
+extern "C" int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
+                                             const double* G, double* Y, double* dX, double* dA,
+                                             double* W, size_t Wcapacity_bytes, int batchCount,
+                                             kmx_stream_t stream) {
+  return kmx::grad_impl<double>(d, n, A, X, G, Y, dX, dA, W, Wcapacity_bytes, batchCount,
+                                reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int kmx_kronmult_batched_grad_f32(int d, int n, const float* A, const float* X,
+                                             const float* G, float* Y, float* dX, float* dA,
+                                             float* W, size_t Wcapacity_bytes, int batchCount,
+                                             kmx_stream_t stream) {
+  return kmx::grad_impl<float>(d, n, A, X, G, Y, dX, dA, W, Wcapacity_bytes, batchCount,
+                               reinterpret_cast<cudaStream_t>(stream));
+}

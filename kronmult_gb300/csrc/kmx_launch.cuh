@@ -29,6 +29,8 @@ struct DeviceInfo {
 };
 
 DeviceInfo device_info(int dev);
+// Device address of the library's status word on the current device (KMX_OK or an error).
+int device_status_ptr(int** out);
 // Raise a kernel's dynamic shared-memory limit once per (kernel, device).
 cudaError_t ensure_smem(const void* func, int dev, size_t bytes);
 

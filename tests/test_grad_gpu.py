@@ -1,0 +1,126 @@
+"""Backward pass: the fused kernel against an explicit-Kronecker gradient,
+FP64 central differences, and torch.autograd.gradcheck."""
+import numpy as np
+import pytest
+
+from tests.common import blockwise_rel_err
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def explicit_grads(A, X, G):
+    """dX, dA of sum(G * (K X)) with K = kron(A_1..A_d) built explicitly.
+    A: (batch, d, n, n) with A[b, l].T the factor (column-major storage)."""
+    batch, d, n, _ = A.shape
+    dX = np.zeros_like(X)
+    dA = np.zeros_like(A)
+    for b in range(batch):
+        mats = [A[b, l].T for l in range(d)]
+        K = mats[0]
+        for m in mats[1:]:
+            K = np.kron(K, m)
+        dX[b] = K.T @ G[b]
+        dK = np.outer(G[b], X[b]).reshape([n] * (2 * d))  # [i_1..i_d, j_1..j_d]
+        for k in range(d):
+            t = dK
+            # contract every mode l != k with A_l(i_l, j_l)
+            letters = "abcdefghijklmnopqrstuvwxyz"
+            ii, jj = letters[:d], letters[d:2 * d]
+            ops, subs = [t], [ii + jj]
+            for l in range(d):
+                if l != k:
+                    ops.append(mats[l])
+                    subs.append(ii[l] + jj[l])
+            g = np.einsum(",".join(subs) + "->" + ii[k] + jj[k], *ops)
+            dA[b, k] = g.T  # column-major storage
+    return dX, dA
+
+
+@pytest.mark.parametrize("d,n", [(1, 3), (2, 4), (3, 3), (4, 2), (3, 5)])
+def test_fused_grad_vs_explicit_kron(kmx, d, n):
+    from kronmult_gb300.autograd import kronmult_fused_grad
+
+    rng = np.random.default_rng(d * 10 + n)
+    batch, N = 3, n ** d
+    A = rng.standard_normal((batch, d, n, n))
+    X = rng.standard_normal((batch, N))
+    G = rng.standard_normal((batch, N))
+    Y, dX, dA = kronmult_fused_grad(*(torch.from_numpy(t).cuda() for t in (A, X, G)))
+    ex_dX, ex_dA = explicit_grads(A, X, G)
+    assert blockwise_rel_err(dX.cpu().numpy(), ex_dX) <= 1e-13
+    assert blockwise_rel_err(dA.cpu().numpy().reshape(batch, -1), ex_dA.reshape(batch, -1)) <= 1e-13
+    # forward output of the fused kernel equals the forward entry point
+    Y2 = torch.zeros_like(Y)
+    kmx.kronmult_batched(d, n, torch.from_numpy(A).cuda(), torch.from_numpy(X).cuda(), Y2, None,
+                         batch, form="plain")
+    assert blockwise_rel_err(Y.cpu().numpy(), Y2.cpu().numpy()) <= 1e-14
+
+
+@pytest.mark.parametrize("d,n,batch", [(6, 5, 3), (3, 8, 8), (6, 4, 4)])
+def test_fused_grad_central_differences(kmx, d, n, batch):
+    """64 random coordinates of X and of each A_i, h = 1e-6: the loss is linear
+    in every single coordinate, so central differences are exact up to rounding."""
+    from kronmult_gb300.autograd import kronmult_fused_grad
+
+    rng = np.random.default_rng(100 + d * n)
+    N = n ** d
+    A = torch.from_numpy(rng.standard_normal((batch, d, n, n)) / np.sqrt(n)).cuda()
+    X = torch.from_numpy(rng.standard_normal((batch, N))).cuda()
+    G = torch.from_numpy(rng.standard_normal((batch, N))).cuda()
+    _, dX, dA = kronmult_fused_grad(A, X, G, want_y=False)
+
+    def loss(Av, Xv):
+        Y = torch.zeros_like(Xv)
+        kmx.kronmult_batched(d, n, Av, Xv, Y, None, batch, form="plain")
+        return float((G * Y).sum())
+
+    h = 1e-6
+    for name, T, grad in [("X", X, dX)] + [(f"A{k}", A, dA) for k in range(d)]:
+        idx = []
+        for _ in range(64):
+            if name == "X":
+                idx.append((int(rng.integers(batch)), int(rng.integers(N))))
+            else:
+                k = int(name[1:])
+                idx.append((int(rng.integers(batch)), k, int(rng.integers(n)), int(rng.integers(n))))
+        for ix in idx:
+            old = float(T[ix])
+            T[ix] = old + h
+            lp = loss(A, X)
+            T[ix] = old - h
+            lm = loss(A, X)
+            T[ix] = old
+            fd = (lp - lm) / (2 * h)
+            g = float(grad[ix])
+            assert abs(fd - g) <= 1e-6 * (1 + abs(g)), (name, ix, fd, g)
+
+
+def test_autograd_function_gradcheck(kmx):
+    from kronmult_gb300.autograd import kronmult
+
+    rng = np.random.default_rng(3)
+    A = torch.from_numpy(rng.standard_normal((2, 3, 2, 2))).cuda().requires_grad_()
+    X = torch.from_numpy(rng.standard_normal((2, 8))).cuda().requires_grad_()
+    assert torch.autograd.gradcheck(lambda a, x: kronmult(a, x, "plain"), (A, X), eps=1e-6,
+                                    atol=1e-8, rtol=1e-6)
+
+
+def test_autograd_backward_matches_fused(kmx):
+    from kronmult_gb300.autograd import kronmult, kronmult_fused_grad
+
+    rng = np.random.default_rng(4)
+    A = torch.from_numpy(rng.standard_normal((5, 4, 3, 3))).cuda().requires_grad_()
+    X = torch.from_numpy(rng.standard_normal((5, 81))).cuda().requires_grad_()
+    G = torch.from_numpy(rng.standard_normal((5, 81))).cuda()
+    Y = kronmult(A, X)
+    Y.backward(G)
+    _, dX, dA = kronmult_fused_grad(A.detach(), X.detach(), G)
+    assert torch.allclose(X.grad, dX, rtol=1e-13, atol=0)
+    assert torch.allclose(A.grad, dA, rtol=1e-13, atol=0)
