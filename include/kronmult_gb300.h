@@ -157,6 +157,23 @@ int kmx_kronmult_vbatched_f32_ex(int d, const int* m, const int* n, const float*
                                  kmx_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Low-precision storage with FP64 accumulation (no counterpart in the     */
+/* reference, whose float path stores and accumulates Y in FP32).          */
+/* ---------------------------------------------------------------------- */
+typedef enum kmx_in_type {
+  KMX_IN_F32 = 1,   /* X and factors stored as FP32 */
+  KMX_IN_BF16 = 2   /* X and factors stored as bfloat16 */
+} kmx_in_type;
+
+/* xbatched with X and factors of in_type, FP32 arithmetic, and each entry's
+ * contribution widened exactly to FP64 and accumulated into FP64 Y blocks
+ * (so many overlapping contributions sum in FP64).  Square n = 2..8 with
+ * d = 3..6, and n = 16 with d = 3. */
+int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aarray, int lda,
+                               const void* const* pX, double* const* pY, int batchCount,
+                               const kmx_options* opt, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Differentiation (no counterpart in the reference, which has no backward).  */
 /* ---------------------------------------------------------------------- */
 

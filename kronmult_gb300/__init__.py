@@ -22,7 +22,7 @@ from ._lib import KmxError, check, exported_symbols, lib, options  # noqa: F401
 __all__ = [
     "KmxError", "lib", "options", "kron_flops", "pointer_array", "check_device_status",
     "kronmult_batched", "kronmult_pbatched", "kronmult_xbatched", "kronmult_vbatched",
-    "set_default_form", "kronmult_mixed",
+    "set_default_form", "kronmult_mixed", "kronmult_xbatched_wide",
 ]
 
 
@@ -176,6 +176,18 @@ def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, bat
         rc = L.kmx_kronmult_vbatched_f32_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
                                             _addr(W), cap, b, _opt(None, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_vbatched")
+
+
+def kronmult_xbatched_wide(d, n, Aarray, lda, pX, pY, batchCount=None, *, in_dtype="f32",
+                           accumulate=None, engine=None, stream=None):
+    """xbatched with FP32 ("f32") or bfloat16 ("bf16") X and factors, FP32
+    arithmetic and FP64 Y accumulation."""
+    code = {"f32": 1, "bf16": 2}[in_dtype]
+    b = batchCount if batchCount is not None else pX.numel()
+    rc = lib().kmx_kronmult_xbatched_wide(code, d, n, _addr(Aarray), lda, _addr(pX), _addr(pY), b,
+                                          _opt(None, accumulate, False, engine),
+                                          C.c_void_p(_stream(stream)))
+    check(rc, f"kronmult{d}_xbatched_wide")
 
 
 def kronmult_mixed(dims, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes=None, *,

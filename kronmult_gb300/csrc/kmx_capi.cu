@@ -159,7 +159,8 @@ static int tuned_form(int d, int n) {
 // ---------------------------------------------------------------------------
 // Common driver: validated Problem -> launcher of the requested form.
 // ---------------------------------------------------------------------------
-static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream_t s) {
+static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream_t s,
+                       int wide_in = 0) {
   if (o.accumulate != KMX_ACC_ATOMIC && o.accumulate != KMX_ACC_DETERMINISTIC)
     return KMX_ERR_INVALID_ARG;
   // Deterministic mode groups entries by Y block.  The contiguous batched
@@ -188,7 +189,7 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     }
     SegArrays sa;
     cudaError_t se = seg_prepare(reinterpret_cast<void* const*>(p.Y), p.count,
-                                 p.Ny * (is_f64 ? 8 : 4), ws, wsb, p.status, s, &sa);
+                                 p.Ny * ((is_f64 || wide_in) ? 8 : 4), ws, wsb, p.status, s, &sa);
     if (se != cudaSuccess) return cuda_fail(se);
     p.seg_entries = sa.entries;
     p.seg_offset = sa.offset;
@@ -206,7 +207,9 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   h.engine = o.engine ? o.engine : engine_env;
   cudaError_t e;
   const bool sq = is_square(p);
-  if (!is_f64) {
+  if (wide_in) {
+    e = wide_in == KMX_IN_BF16 ? launch_wide_bf16(p, h, s) : launch_wide_f32(p, h, s);
+  } else if (!is_f64) {
     if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
     e = launch_f32_plain(p, h, s);
   } else {
@@ -387,6 +390,29 @@ static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarr
   return run_problem(p, sizeof(T) == 8, o, s);
 }
 
+// xbatched with FP32/BF16 inputs and an FP64 Y (register-tiled shapes).
+static int xbatched_wide_impl(int in_type, int d, int n, const void* const* Aarray, int lda,
+                              const void* const* pX, double* const* pY, int batch,
+                              const kmx_options* opt, cudaStream_t s) {
+  if (in_type != KMX_IN_F32 && in_type != KMX_IN_BF16) return KMX_ERR_INVALID_ARG;
+  if (d < 1 || d > MAXD || n < 1 || batch < 0) return KMX_ERR_INVALID_ARG;
+  if (lda == 0) lda = n;
+  if (lda < n) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!Aarray || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  long long N;
+  if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  base_square(p, L_XBATCHED, d, n, lda, N);
+  p.count = batch;
+  p.A = Aarray;
+  p.X = pX;
+  p.Y = const_cast<double**>(pY);
+  p.trans = o.transpose;
+  return run_problem(p, false, o, s, in_type);
+}
+
 // One call over instances of mixed (d, n): group by class on the device,
 // then one tuned launch per class reading its range from device memory.
 template <typename T>
@@ -561,6 +587,13 @@ int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarra
                            const kmx_options* opt, kmx_stream_t stream) {
   return mixed_impl<float>(count, dims, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
                            nclasses, opt, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aarray, int lda,
+                               const void* const* pX, double* const* pY, int batchCount,
+                               const kmx_options* opt, kmx_stream_t stream) {
+  return xbatched_wide_impl(in_type, d, n, Aarray, lda, pX, pY, batchCount, opt,
+                            KMX_STREAM(stream));
 }
 
 size_t kmx_deterministic_workspace_bytes(int batchCount) {

@@ -8,4 +8,6 @@ struct LaunchHint;
 cudaError_t launch_f64_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f64_split(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
+cudaError_t launch_wide_f32(Problem& p, const LaunchHint& h, cudaStream_t s);
+cudaError_t launch_wide_bf16(Problem& p, const LaunchHint& h, cudaStream_t s);
 }  // namespace kmx

@@ -12,7 +12,7 @@
 
 namespace kmx {
 
-enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2 };
+enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2, FORM_WIDE = 3 };
 
 // Execution shape requested by the caller (0 = choose).
 struct LaunchHint {
@@ -89,6 +89,11 @@ template <typename T>
 struct TilePol<T, FORM_SPLIT> {
   using type = tile::SplitPolicy;
 };
+// FP32 / BF16 storage, FP32 arithmetic, FP64 Y (T is the storage type)
+template <typename T>
+struct TilePol<T, FORM_WIDE> {
+  using type = tile::WidePolicy<T>;
+};
 
 struct TileKernel {
   const void* func = nullptr;
@@ -132,6 +137,7 @@ TileKernel pick_tile(int nn, int d) {
     case 6: return tile_for_d<T, FORM, 6, SEG>(d);
     case 7: return tile_for_d<T, FORM, 7, SEG>(d);
     case 8: return tile_for_d<T, FORM, 8, SEG>(d);
+    case 16: return d == 3 ? tile_entry<T, FORM, 16, 3, SEG>() : TileKernel();
     default: return TileKernel();
   }
 }
@@ -207,6 +213,9 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
     const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
     if (tk.func) return launch_tile(p, tk, hint, stream);
   }
+  if constexpr (FORM == FORM_WIDE) {
+    return cudaErrorNotSupported;  // register-tiled shapes only (handled above)
+  } else {
   const bool spec = square && pick_sq<T, FORM, false>(nn) != nullptr;
   // FORM_SPLIT exists for specialised square shapes only; others run plain.
   if (FORM == FORM_SPLIT && !spec) return cudaErrorNotSupported;
@@ -254,6 +263,7 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   p.group_smem = (int)gsm;
   void* args[] = {&p};
   return cudaLaunchKernel(func, dim3(grid), dim3(E * G), args, smem, stream);
+  }
 }
 
 }  // namespace kmx

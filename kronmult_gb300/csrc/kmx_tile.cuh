@@ -22,6 +22,10 @@
 // different (but equally valid) order of the mode products.
 #pragma once
 
+#include <cuda_bf16.h>
+
+#include <type_traits>
+
 #include "kmx_engine.cuh"
 
 namespace kmx {
@@ -53,14 +57,17 @@ __host__ __device__ constexpr int tile_size(int NN, int D, int p) {
 }
 
 // threads per entry: one tile per thread in the first phase where possible
-// (at most 512), and at least one thread per factor entry (d*NN*NN)
+// (32..512); a thread may own several factor entries (factors_per_thread)
 __host__ __device__ constexpr int round32(int x) { return (x + 31) / 32 * 32; }
 __host__ __device__ constexpr int group_threads(int NN, int D) {
   return round32(ipow(NN, D) / tile_size(NN, D, 0)) > 512
-             ? (round32(D * NN * NN) > 512 ? round32(D * NN * NN) : 512)
-             : (round32(ipow(NN, D) / tile_size(NN, D, 0)) < round32(D * NN * NN)
-                    ? round32(D * NN * NN)
+             ? 512
+             : (round32(ipow(NN, D) / tile_size(NN, D, 0)) < 32
+                    ? 32
                     : round32(ipow(NN, D) / tile_size(NN, D, 0)));
+}
+__host__ __device__ constexpr int factors_per_thread(int NN, int D) {
+  return (D * NN * NN + group_threads(NN, D) - 1) / group_threads(NN, D);
 }
 
 // physical slot of logical element q in the shared intermediate
@@ -175,6 +182,32 @@ struct PlainPolicy {
     return acc;
   }
   __device__ __forceinline__ static T finish(V o, int) { return o; }
+};
+
+// Low-precision storage with FP32 arithmetic and FP64 results: X and the
+// factors are FP32 or BF16 (converted exactly to FP32), the d mode products
+// run in FP32, and each contribution is widened exactly to FP64 before it is
+// added to the (FP64) Y block, so overlapping contributions accumulate in FP64.
+template <typename TIn>
+struct WidePolicy {
+  using In = TIn;
+  using V = float;
+  using Out = double;
+  static constexpr bool SCALED = false;
+  __device__ __forceinline__ static V make(TIn x, int) { return to_f32(x); }
+  __device__ __forceinline__ static float to_f32(float x) { return x; }
+  __device__ __forceinline__ static float to_f32(__nv_bfloat16 x) {
+    return __uint_as_float(((unsigned)__bfloat16_as_ushort(x)) << 16);
+  }
+  template <int NN>
+  __device__ __forceinline__ static V dot(const V* a, const V* v) {
+    V acc = a[0] * v[0];
+#pragma unroll
+    for (int j = 1; j < NN; ++j) acc = fmaf(a[j], v[j], acc);
+    return acc;
+  }
+  // exact FP32 -> FP64 by exponent arithmetic (no conversion instruction)
+  __device__ __forceinline__ static double finish(V o, int) { return SplitPolicy::to_f64(o, 0); }
 };
 
 // Contract the tile's mode(s) in registers.  sA points at the phase's
@@ -483,15 +516,20 @@ tile_kernel(const Problem p) {
   group_sync(g, G);
   if (!(sDesc[0].flags & ED_VALID)) return;  // nothing for this group (uniform)
 
-  // factor entry owned by this thread (one per thread: G >= D*NN*NN)
-  const bool fthr = lt < D * NN2;
-  const int al = fthr ? lt / NN2 : 0;
-  const int ar = fthr ? (lt - al * NN2) / NN : 0;
-  const int aj = fthr ? lt - al * NN2 - ar * NN : 0;
-  const int ald = p.ld[al];
-  auto fetch_factor = [&](const In* Ap) -> In {
-    return p.trans ? Ap[aj + (long long)ar * ald] : Ap[ar + (long long)aj * ald];
-  };
+  // factor entries owned by this thread: lt, lt + G, ... below d*NN*NN
+  constexpr int FPT = factors_per_thread(NN, D);
+  bool fthr[FPT];
+  int al[FPT], aoff[FPT];
+#pragma unroll
+  for (int f = 0; f < FPT; ++f) {
+    const int idx = lt + f * G;
+    fthr[f] = idx < D * NN2;
+    al[f] = fthr[f] ? idx / NN2 : 0;
+    const int ar = fthr[f] ? (idx - al[f] * NN2) / NN : 0;
+    const int aj = fthr[f] ? idx - al[f] * NN2 - ar * NN : 0;
+    const int ald = p.ld[al[f]];
+    aoff[f] = p.trans ? aj + ar * ald : ar + aj * ald;
+  }
   uint32_t uses = 0;  // thread 0: completed phases of the barrier
   auto issue_x = [&](const In* xsrc) {
     int mode = 0;
@@ -504,17 +542,21 @@ tile_kernel(const Problem p) {
     sMode[0] = mode;
   };
 
-  // ---- prologue: first entry's factor entry and scale, its X block ----
-  In af = In(0);
+  // ---- prologue: first entry's factor entries and scales, its X block ----
+  In af[FPT];
   {
     const long long ent = sDesc[0].ent;
-    if (fthr) {
-      const In* Ap = a_ptr<In>(p, ent, al);
-      if (Ap) {
-        af = fetch_factor(Ap);
-        if constexpr (Pol::SCALED) atomicMax(&sExp[al], exp_field(af));
-      } else {
-        atomicOr(&sFlag[0], TF_NULL);
+#pragma unroll
+    for (int f = 0; f < FPT; ++f) {
+      af[f] = In(0);
+      if (fthr[f]) {
+        const In* Ap = a_ptr<In>(p, ent, al[f]);
+        if (Ap) {
+          af[f] = Ap[aoff[f]];
+          if constexpr (Pol::SCALED) atomicMax(&sExp[al[f]], exp_field(af[f]));
+        } else {
+          atomicOr(&sFlag[0], TF_NULL);
+        }
       }
     }
     if (lt == 0) issue_x(x_ptr<In>(p, ent));
@@ -528,7 +570,7 @@ tile_kernel(const Problem p) {
     int* ex_k = sExp + pb * (MAXD + 1);
     int* ex_n = sExp + (pb ^ 1) * (MAXD + 1);
     const long long ent = dk.ent;
-    In* yp = y_ptr<In>(p, ent);
+    Out* yp = y_ptr<Out>(p, ent);
     const In* xnext = nullptr;
     if (lt == 0) {
       EntryDesc dn;
@@ -536,7 +578,9 @@ tile_kernel(const Problem p) {
       sDesc[pb ^ 1] = dn;
       if (dn.flags & ED_VALID) xnext = x_ptr<In>(p, dn.ent);
     }
-    if (fthr) sA[lt] = Pol::make(af, Pol::SCALED ? ex_k[al] : 0);
+#pragma unroll
+    for (int f = 0; f < FPT; ++f)
+      if (fthr[f]) sA[lt + f * G] = Pol::make(af[f], Pol::SCALED ? ex_k[al[f]] : 0);
     if (lt <= MAXD) ex_n[lt] = 0;
     if (lt == 0) {
       sFlag[pb ^ 1] = 0;
@@ -557,20 +601,28 @@ tile_kernel(const Problem p) {
     const bool has_next = (dn.flags & ED_VALID) != 0;
     const bool first = (dk.flags & ED_FIRST) != 0;
     const bool last = !has_next || (dn.flags & ED_FIRST);
-    const In* anext = (has_next && fthr) ? a_ptr<In>(p, dn.ent, al) : nullptr;
+    const In* anext[FPT];
+#pragma unroll
+    for (int f = 0; f < FPT; ++f)
+      anext[f] = (has_next && fthr[f]) ? a_ptr<In>(p, dn.ent, al[f]) : nullptr;
 
     auto fetch_next_factor = [&]() {
-      if (fthr && has_next) {
-        if (anext) {
-          af = fetch_factor(anext);
-        } else {
-          atomicOr(&sFlag[pb ^ 1], TF_NULL);
+#pragma unroll
+      for (int f = 0; f < FPT; ++f) {
+        if (fthr[f] && has_next) {
+          if (anext[f]) {
+            af[f] = anext[f][aoff[f]];
+          } else {
+            atomicOr(&sFlag[pb ^ 1], TF_NULL);
+          }
         }
       }
     };
     auto reduce_next_scale = [&]() {
       if constexpr (Pol::SCALED) {
-        if (fthr && has_next && anext) atomicMax(&ex_n[al], exp_field(af));
+#pragma unroll
+        for (int f = 0; f < FPT; ++f)
+          if (fthr[f] && has_next && anext[f]) atomicMax(&ex_n[al[f]], exp_field(af[f]));
       }
     };
     // Deterministic mode, an entry without a contribution: keep the
@@ -644,7 +696,7 @@ tile_kernel(const Problem p) {
       }
       if (skip || nonfinite) {
         if (!ONE && lt == 0 && has_next) issue_x(xnext);
-        if constexpr (sizeof(In) == 8) {
+        if constexpr (std::is_same<In, double>::value) {
           // Inf/NaN propagate exactly as in FP64: plain FP64 on the same
           // shared memory (an all-zero factor or X contributes exactly zero).
           if (nonfinite) {

@@ -538,3 +538,37 @@ def test_cuda_graph_of_repeated_mixed_calls(kmx, oracle):
     torch.cuda.synchronize()
     assert blockwise_rel_err(host(y_graph), host(y_eager)) <= 1e-12
     check_status(kmx)
+
+
+# ---------------------------------------------------------------------------
+# FP32 / BF16 storage with FP64 accumulation into shared Y blocks
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("in_dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("d,n", [(4, 8), (3, 16), (6, 4), (3, 5)])
+@pytest.mark.parametrize("acc", ["atomic", "deterministic"])
+def test_wide_forms_vs_fp64_oracle(kmx, oracle, in_dtype, d, n, acc):
+    """The FP64 oracle runs on the same (rounded) inputs, so the error measures
+    the FP32 arithmetic only; FP64 Y accumulation keeps it at FP32 level."""
+    rng = np.random.default_rng(61 + d * n)
+    pool, nx, ny, ne = 40, 30, 12, 400
+    N = n ** d
+    tdt = torch.float32 if in_dtype == "f32" else torch.bfloat16
+    Apool = torch.from_numpy(rng.standard_normal((d, pool, n, n)) / np.sqrt(n)).to(tdt).cuda()
+    Xpool = torch.from_numpy(rng.standard_normal((nx, N))).to(tdt).cuda()
+    Y0 = rng.standard_normal((ny, N))
+    y_idx = rng.geometric(1 / 16, ne) % ny
+    x_idx = rng.integers(0, nx, ne)
+    a_idx = rng.integers(0, pool, (ne, d))
+    Yref = Y0.copy()
+    oracle.xbatched_idx(d, n, Apool.double().cpu().numpy(), n, pool, Xpool.double().cpu().numpy(),
+                        Yref, y_idx, x_idx, a_idx)
+    esz = Apool.element_size()
+    pA = kmx.pointer_array(Apool, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel(), esz)
+    pX = kmx.pointer_array(Xpool, x_idx * N, esz)
+    Yd = dev(Y0)
+    pY = kmx.pointer_array(Yd, y_idx * N)
+    kmx.kronmult_xbatched_wide(d, n, pA, n, pX, pY, ne, in_dtype=in_dtype, accumulate=acc)
+    err = blockwise_rel_err(host(Yd), Yref)
+    assert err <= 2e-6, err
+    check_status(kmx)
