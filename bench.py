@@ -426,6 +426,215 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Secondary workloads (one JSON line each; the default run is the headline).
+# ---------------------------------------------------------------------------
+
+def _events_time(torch, fn, K, W):
+    for _ in range(W):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / K
+
+
+def _blockwise_err(torch, y, yref, rows):
+    """max over blocks of the normwise relative error (blocks given as slices)."""
+    worst = 0.0
+    for a, b in rows:
+        r = yref[a:b]
+        s = r.abs().max().clamp_min(1e-300)
+        num = torch.linalg.vector_norm((y[a:b] - r) / s)
+        den = torch.linalg.vector_norm(r / s).clamp_min(1e-300)
+        worst = max(worst, float(num / den))
+    return worst
+
+
+def run_mixed(args):
+    """65536 instances, d ~ U{1..6}, n ~ U{2,3,4,5,6,8}, n^d <= 262144, own
+    factors, X and Y ~ U[-1,1]; one kronmult_mixed call per step, a 100-call
+    sequence captured as a CUDA graph and replayed."""
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    rng = np.random.default_rng(SEED + 3)
+    count = args.entries if args.entries != ENTRIES else 65536
+    d = rng.integers(1, 7, count)
+    n = rng.choice(np.array([2, 3, 4, 5, 6, 8]), count)
+    bad = n.astype(np.float64) ** d > 262144
+    while bad.any():
+        d[bad] = rng.integers(1, 7, bad.sum())
+        n[bad] = rng.choice(np.array([2, 3, 4, 5, 6, 8]), bad.sum())
+        bad = n.astype(np.float64) ** d > 262144
+    N = n.astype(np.int64) ** d
+    xoff = np.concatenate([[0], np.cumsum(N)[:-1]])
+    nf = d.astype(np.int64)
+    a_off = np.concatenate([[0], np.cumsum(nf)[:-1]])
+    fsz = np.repeat(n.astype(np.int64) ** 2, nf)
+    foff = np.concatenate([[0], np.cumsum(fsz)[:-1]])
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(SEED)
+    X = torch.rand(int(N.sum()), dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    Y = torch.rand(int(N.sum()), dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    F = torch.rand(int(fsz.sum()), dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    dims = torch.from_numpy(np.stack([d, n], 1).astype(np.int32)).to(dev)
+    pA = torch.from_numpy(foff).to(dev) * 8 + F.data_ptr()
+    pX = torch.from_numpy(xoff).to(dev) * 8 + X.data_ptr()
+    pY = torch.from_numpy(xoff).to(dev) * 8 + Y.data_ptr()
+    aoff_d = torch.from_numpy(a_off).to(dev)
+    classes = sorted({(int(a), int(b)) for a, b in zip(d, n)}, key=lambda c: -(c[0] * c[1] ** (c[0] + 1)))
+    W = torch.empty(2 * 262144 * 512, dtype=torch.float64, device=dev)
+    flops = float((2.0 * d * n.astype(np.float64) ** (d + 1)).sum())
+    res = {}
+    for form in ("auto", "plain"):
+        call = lambda: kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form)
+        ms_eager = _events_time(torch, call, max(2, args.steps // 3), 2)
+        # 100-call sequence as one CUDA graph
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(graph, stream=s):
+                for _ in range(100):
+                    kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form, stream=s)
+        torch.cuda.current_stream().wait_stream(s)
+        ms_graph = _events_time(torch, graph.replay, 2, 1) / 100
+        res[form] = {"gflops_graph": round(flops / (ms_graph * 1e-3) / 1e9, 2),
+                     "ms_per_call_graph": round(ms_graph, 4),
+                     "gflops_eager": round(flops / (ms_eager * 1e-3) / 1e9, 2),
+                     "ms_per_call_eager": round(ms_eager, 4)}
+    # accuracy of the chosen form against plain FP64 on fresh Y
+    Yc = torch.zeros_like(Y)
+    Yp = torch.zeros_like(Y)
+    kmx.kronmult_mixed(dims, pA, aoff_d, pX, torch.from_numpy(xoff).to(dev) * 8 + Yc.data_ptr(),
+                       classes, W)
+    kmx.kronmult_mixed(dims, pA, aoff_d, pX, torch.from_numpy(xoff).to(dev) * 8 + Yp.data_ptr(),
+                       classes, W, form="plain")
+    torch.cuda.synchronize()
+    kmx.check_device_status()
+    pick = rng.choice(count, 512, replace=False)
+    err = _blockwise_err(torch, Yc, Yp, [(int(xoff[i]), int(xoff[i] + N[i])) for i in pick])
+    print(json.dumps({"metric": "kronmult GFLOP/s, mixed-shape batch (one call), FP64",
+                      "value": res["auto"]["gflops_graph"], "unit": "GFLOP/s", "n_gpus": 1,
+                      "workload": "mixed", "instances": count, "classes": len(classes),
+                      "total_gflop_per_call": round(flops / 1e9, 2),
+                      "chosen": res["auto"], "plain": res["plain"],
+                      "rel_err_chosen_vs_plain_512_instances": err, "data": "synthetic"}))
+
+
+def run_grad(args):
+    """Fused forward+backward against forward alone: d=6 n=5 batch 1024 and
+    d=3 n=8 batch 4096 (FP64)."""
+    import torch
+
+    import kronmult_gb300 as kmx
+    from kronmult_gb300.autograd import _grad_call, grad_workspace
+
+    out = []
+    for d, n, batch in ((6, 5, 1024), (3, 8, 4096)):
+        N = n ** d
+        g = torch.Generator(device="cuda").manual_seed(SEED + d)
+        A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
+        X = torch.randn((batch, N), dtype=torch.float64, device="cuda", generator=g)
+        G = torch.randn((batch, N), dtype=torch.float64, device="cuda", generator=g)
+        Y = torch.zeros_like(X)
+        dX = torch.zeros_like(X)
+        dA = torch.zeros_like(A)
+        W = grad_workspace(d, n, batch)
+        fwd = {}
+        for form in ("plain", "split"):
+            fwd[form] = _events_time(torch, lambda: kmx.kronmult_batched(d, n, A, X, Y, None, batch, form=form),
+                                     args.steps, 3)
+        both = _events_time(torch, lambda: _grad_call(d, n, A, X, G, Y, dX, dA, W), args.steps, 3)
+        fl = batch * 2.0 * d * n ** (d + 1)
+        out.append({"d": d, "n": n, "batch": batch, "fwd_plain_ms": round(fwd["plain"], 4),
+                    "fwd_split_ms": round(fwd["split"], 4), "fwd_bwd_ms": round(both, 4),
+                    "ratio_vs_plain_fwd": round(both / fwd["plain"], 3),
+                    "ratio_vs_chosen_fwd": round(both / fwd["split"], 3),
+                    "fwd_plain_gflops": round(fl / (fwd["plain"] * 1e-3) / 1e9, 1)})
+    kmx.check_device_status()
+    print(json.dumps({"metric": "fused forward+backward time / forward time (FP64)",
+                      "value": out[0]["ratio_vs_plain_fwd"], "unit": "ratio", "workload": "grad",
+                      "cases": out, "data": "synthetic"}))
+
+
+def run_precision(args):
+    """xbatched d=4 n=8 and d=3 n=16, 262144 entries over 16384 X/Y blocks,
+    geometric(16) per-Y counts, factors N(0,1)/sqrt(n), X N(0,1): FP64 forms,
+    FP32- and BF16-stored forms with FP64 Y; errors against plain FP64."""
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    entries = args.entries if args.entries != ENTRIES else 262144
+    nblocks = 16384
+    out = []
+    for d, n in ((4, 8), (3, 16)):
+        N = n ** d
+        rng = np.random.default_rng(SEED + 11 * n)
+        counts = rng.geometric(1.0 / 16, nblocks)
+        y_idx = np.repeat(np.arange(nblocks), counts)[:entries]
+        if len(y_idx) < entries:
+            y_idx = np.concatenate([y_idx, rng.integers(0, nblocks, entries - len(y_idx))])
+        rng.shuffle(y_idx)
+        x_idx = rng.integers(0, nblocks, entries)
+        pool = 1024
+        a_idx = rng.integers(0, pool, (entries, d))
+        g = torch.Generator(device="cuda").manual_seed(SEED + n)
+        A64 = torch.randn((d, pool, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
+        X64 = torch.randn((nblocks, N), dtype=torch.float64, device="cuda", generator=g)
+        lvl = torch.arange(d, device="cuda")[None, :]
+        ai = torch.from_numpy(a_idx).cuda()
+        xi = torch.from_numpy(x_idx).cuda()
+        yi = torch.from_numpy(y_idx).cuda()
+
+        def ptrs(A, X, Y):
+            e = A.element_size()
+            return (((lvl * pool + ai) * (n * n * e) + A.data_ptr()).reshape(-1).contiguous(),
+                    xi * (N * X.element_size()) + X.data_ptr(), yi * (N * 8) + Y.data_ptr())
+
+        fl = entries * 2.0 * d * n ** (d + 1)
+        res = {}
+        Yref = torch.zeros((nblocks, N), dtype=torch.float64, device="cuda")
+        pA, pX, pY = ptrs(A64, X64, Yref)
+        kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, entries, form="plain")
+        Yacc = torch.zeros_like(Yref)
+        for name in ("plain", "split", "f32", "bf16"):
+            if name in ("plain", "split"):
+                A, X = A64, X64
+            else:
+                tdt = torch.float32 if name == "f32" else torch.bfloat16
+                A, X = A64.to(tdt), X64.to(tdt)
+            pA, pX, pY = ptrs(A, X, Yacc)
+            if name in ("plain", "split"):
+                call = lambda: kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, entries, form=name)
+            else:
+                call = lambda: kmx.kronmult_xbatched_wide(d, n, pA, n, pX, pY, entries, in_dtype=name)
+            ms = _events_time(torch, call, max(3, args.steps // 2), 2)
+            Yacc.zero_()
+            call()
+            torch.cuda.synchronize()
+            s = Yref.abs().amax(dim=1, keepdim=True).clamp_min(1e-300)
+            err = float((torch.linalg.vector_norm((Yacc - Yref) / s, dim=1) /
+                         torch.linalg.vector_norm(Yref / s, dim=1).clamp_min(1e-300)).max())
+            res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                         "rel_err_vs_fp64_gpu": err}
+        out.append({"d": d, "n": n, "entries": entries, "forms": res,
+                    "f32_speedup_vs_fp64_plain": round(res["plain"]["ms"] / res["f32"]["ms"], 2),
+                    "f32_speedup_vs_fp64_chosen": round(res["split"]["ms"] / res["f32"]["ms"], 2)})
+    kmx.check_device_status()
+    print(json.dumps({"metric": "kronmult precision forms, xbatched (GFLOP/s and error vs FP64)",
+                      "value": out[0]["f32_speedup_vs_fp64_chosen"], "unit": "ratio",
+                      "workload": "precision", "cases": out, "data": "synthetic"}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -435,9 +644,17 @@ def main():
     ap.add_argument("--entries", type=int, default=ENTRIES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["xbatched", "mixed", "grad", "precision"],
+                    default="xbatched")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "mixed":
+        return run_mixed(args)
+    if args.workload == "grad":
+        return run_grad(args)
+    if args.workload == "precision":
+        return run_precision(args)
     return run_ours(args)
 
 

@@ -186,6 +186,11 @@ int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aar
  * are (n^d, batch).  Square n = 2..8.  W (Wcapacity_bytes) holds (d-1)*n^d
  * elements per concurrent entry when the intermediates exceed shared memory
  * (about 200 KB per entry); otherwise it may be NULL. */
+/* Workspace bytes the fused kernel wants for (d, n, batchCount) on the current
+ * device: 0 when the intermediates fit in shared memory (W may be NULL);
+ * otherwise slots for the concurrently processed entries. */
+size_t kmx_grad_workspace_bytes(int d, int n, int batchCount, int fp64);
+
 int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
                                   const double* G, double* Y, double* dX, double* dA,
                                   double* W, size_t Wcapacity_bytes, int batchCount,

@@ -114,6 +114,8 @@ def lib():
             L.kmx_kron_flops.restype = C.c_double
             L.kmx_status_string.argtypes = [_i]
             L.kmx_status_string.restype = C.c_char_p
+            L.kmx_grad_workspace_bytes.argtypes = [_i, _i, _i, _i]
+            L.kmx_grad_workspace_bytes.restype = C.c_size_t
             L.kmx_deterministic_workspace_bytes.argtypes = [_i]
             L.kmx_deterministic_workspace_bytes.restype = C.c_size_t
             L.kmx_version.argtypes = []

@@ -33,14 +33,14 @@ def _grad_call(d, n, A, X, G, Y, dX, dA, W):
 
 
 def grad_workspace(d, n, batch, dtype=torch.float64, device="cuda"):
-    """Workspace for the fused backward when an entry's intermediates exceed
-    shared memory (one slot per concurrently processed entry)."""
-    N = n ** d
-    esz = 8 if dtype == torch.float64 else 4
-    if 2 * 6 * n * n * esz + N * esz * max(d, 1) <= 200 * 1024:
+    """Workspace for the fused backward (None when an entry's intermediates
+    fit in shared memory); the library reports the size it wants."""
+    f64 = dtype == torch.float64
+    nbytes = _lib.lib().kmx_grad_workspace_bytes(d, n, batch, 1 if f64 else 0)
+    if nbytes == 0:
         return None
-    slots = min(batch, 304)
-    return torch.empty(slots * max(d - 1, 1) * N, dtype=dtype, device=device)
+    esz = 8 if f64 else 4
+    return torch.empty((nbytes + esz - 1) // esz, dtype=dtype, device=device)
 
 
 def kronmult_fused_grad(A, X, G, want_y=True):

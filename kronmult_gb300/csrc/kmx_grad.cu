@@ -64,39 +64,71 @@ __device__ __forceinline__ void mode_apply(const T* src, T* dst, const T* A, boo
   }
 }
 
-// Gram along the mode of stride s: dA(a, b) += sum_fibers B[a] * Fk[b].
+// Gram along the mode of stride s: dA(a, b) += sum over fibers B[a] * Fk[b].
+//
+// NN <= 5: a thread owns whole fibers, loads each fiber's NN values of B and
+// of Fk once (Fk may live in global memory) and accumulates all NN^2 products
+// in registers.  The G x NN^2 partial sums are then reduced through shared
+// memory (sRed: NN^2 x G, sRed2: NN^2 x G/32) with one FP64 add per partial --
+// a shuffle tree would spend five adds per partial on the narrow FP64 pipe.
+// NN > 5 (NN^2 accumulators would not fit in registers): thread t owns the
+// pair (a, b) = t mod NN^2 and every (G / NN^2)-th fiber; one atomic each.
 template <typename T, int NN>
-__device__ __forceinline__ void mode_gram(const T* B, const T* Fk, T* sdA, int s, int F, int lt,
-                                          int G) {
-  constexpr int ROWS = NN <= 5 ? NN : 2;
+__device__ __forceinline__ void mode_gram(const T* B, const T* Fk, T* sdA, T* sRed, int s, int F,
+                                          int lt, int G) {
+  constexpr int NN2 = NN * NN;
   const FastDiv fd((unsigned)s);
-  for (int r0 = 0; r0 < NN; r0 += ROWS) {
-    T acc[ROWS][NN];
+  if constexpr (NN <= 5) {
+    T acc[NN2];
 #pragma unroll
-    for (int a = 0; a < ROWS; ++a)
-#pragma unroll
-      for (int b = 0; b < NN; ++b) acc[a][b] = T(0);
+    for (int q = 0; q < NN2; ++q) acc[q] = T(0);
     for (int f = lt; f < F; f += G) {
       const unsigned o = fd((unsigned)f);
       const int r = f - (int)o * s;
       const long long base = (long long)o * NN * s + r;
-      T x[NN];
+      T bv[NN], x[NN];
 #pragma unroll
-      for (int b = 0; b < NN; ++b) x[b] = Fk[base + (long long)b * s];
-#pragma unroll
-      for (int a = 0; a < ROWS; ++a) {
-        if (r0 + a < NN) {
-          const T bv = B[base + (long long)(r0 + a) * s];
-#pragma unroll
-          for (int b = 0; b < NN; ++b) acc[a][b] = fma(bv, x[b], acc[a][b]);
-        }
+      for (int j = 0; j < NN; ++j) {
+        bv[j] = B[base + (long long)j * s];
+        x[j] = Fk[base + (long long)j * s];
       }
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int b = 0; b < NN; ++b) acc[a * NN + b] = fma(bv[a], x[b], acc[a * NN + b]);
     }
 #pragma unroll
-    for (int a = 0; a < ROWS; ++a)
-      if (r0 + a < NN)
-#pragma unroll
-        for (int b = 0; b < NN; ++b) atomicAdd(&sdA[(r0 + a) * NN + b], acc[a][b]);
+    for (int q = 0; q < NN2; ++q) sRed[q * G + lt] = acc[q];
+    __syncthreads();
+    const int nch = G / 32;
+    T* sRed2 = sRed + NN2 * G;
+    for (int t = lt; t < NN2 * nch; t += G) {
+      const int q = t / nch, c = t - q * nch;
+      const T* src = sRed + q * G + c * 32;
+      T v = src[0];
+#pragma unroll 8
+      for (int i = 1; i < 32; ++i) v += src[i];
+      sRed2[t] = v;
+    }
+    __syncthreads();
+    for (int q = lt; q < NN2; q += G) {
+      T v = sRed2[q * nch];
+      for (int c = 1; c < nch; ++c) v += sRed2[q * nch + c];
+      sdA[q] += v;
+    }
+  } else {
+    const int chunks = G / NN2;
+    if (lt >= chunks * NN2) return;
+    const int pr = lt % NN2, c0 = lt / NN2;
+    const int a = pr / NN, b = pr - a * NN;
+    T acc = T(0);
+    for (int f = c0; f < F; f += chunks) {
+      const unsigned o = fd((unsigned)f);
+      const int r = f - (int)o * s;
+      const long long base = (long long)o * NN * s + r;
+      acc = fma(B[base + (long long)a * s], Fk[base + (long long)b * s], acc);
+    }
+    atomicAdd(&sdA[pr], acc);
   }
 }
 
@@ -110,7 +142,8 @@ __global__ void __launch_bounds__(256) grad_kernel(const GradProblem gp) {
   T* sA = reinterpret_cast<T*>(smem);
   T* sdA = sA + MAXD * NN2;
   T* sB = sdA + MAXD * NN2;
-  T* sF = sB + N;  // (d-1) forward intermediates when they fit
+  T* sRed = sB + N;                                            // Gram partial sums (NN <= 5)
+  T* sF = sRed + (NN <= 5 ? NN2 * (G + G / 32) : 0);           // forward intermediates, if they fit
   const long long slot = blockIdx.x;
   T* Fst = gp.f_in_smem ? sF
                         : (gp.W ? static_cast<T*>(gp.W) + slot * gp.wslot : nullptr);
@@ -154,7 +187,7 @@ __global__ void __launch_bounds__(256) grad_kernel(const GradProblem gp) {
     s = 1;
     for (int k = d - 1; k >= 0; --k, s *= NN) {
       const T* Fk = k == 0 ? Xe : Fst + (long long)(k - 1) * N;
-      if (gp.dA) mode_gram<T, NN>(sB, Fk, sdA + k * NN2, s, F, lt, G);
+      if (gp.dA) mode_gram<T, NN>(sB, Fk, sdA + k * NN2, sRed, s, F, lt, G);
       if (k > 0) {
         __syncthreads();  // the Gram read sB before it is overwritten
         mode_apply<T, NN>(sB, sB, sA + k * NN2, true, s, F, lt, G);
@@ -211,6 +244,39 @@ const void* pick_grad(int n) {
   }
 }
 
+// Launch shape and memory plan of the fused kernel for (d, n).
+struct GradPlan {
+  int threads;
+  size_t smem;
+  int f_in_smem;
+  size_t slot_bytes;  // workspace per concurrent entry when !f_in_smem
+  bool ok;
+};
+
+template <typename T>
+GradPlan grad_plan(int d, int n, long long N, int max_smem) {
+  GradPlan g;
+  int threads = (int)((N / n + 31) / 32 * 32);
+  if (threads < 64) threads = 64;
+  if (threads > 256) threads = 256;
+  g.threads = threads;
+  const size_t red = n <= 5 ? (size_t)n * n * (threads + threads / 32) * sizeof(T) : 0;
+  const size_t head = 2 * (size_t)MAXD * n * n * sizeof(T) + red;
+  const size_t with_f = head + (size_t)N * sizeof(T) * (d > 1 ? d : 1);
+  const size_t without_f = head + (size_t)N * sizeof(T);
+  g.slot_bytes = (size_t)(d > 1 ? d - 1 : 1) * N * sizeof(T);
+  if (with_f <= 200 * 1024) {
+    g.f_in_smem = 1;
+    g.smem = with_f;
+    g.ok = true;
+  } else {
+    g.f_in_smem = 0;
+    g.smem = without_f;
+    g.ok = without_f <= (size_t)max_smem;
+  }
+  return g;
+}
+
 template <typename T>
 int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* dA, T* W,
               size_t Wbytes, int batch, cudaStream_t s) {
@@ -237,20 +303,15 @@ int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* 
   gp.dA = dA;
   gp.W = W;
   gp.wslot = (long long)(d > 1 ? d - 1 : 1) * N;
-  const size_t head = 2 * (size_t)MAXD * n * n * sizeof(T);
-  const size_t with_f = head + (size_t)N * sizeof(T) * (d > 1 ? d : 1);
-  const size_t without_f = head + (size_t)N * sizeof(T);
-  size_t smem;
-  if (with_f <= 200 * 1024) {
-    gp.f_in_smem = 1;
-    smem = with_f;
+  const GradPlan plan = grad_plan<T>(d, n, N, di.max_smem_optin);
+  if (!plan.ok) return KMX_ERR_UNSUPPORTED;
+  const int threads = plan.threads;
+  const size_t smem = plan.smem;
+  gp.f_in_smem = plan.f_in_smem;
+  if (plan.f_in_smem) {
     gp.nslots = batch;
   } else {
-    if (without_f > (size_t)di.max_smem_optin) return KMX_ERR_UNSUPPORTED;
-    gp.f_in_smem = 0;
-    smem = without_f;
-    const size_t slot_bytes = (size_t)gp.wslot * sizeof(T);
-    gp.nslots = W ? (int)(Wbytes / slot_bytes < (size_t)batch ? Wbytes / slot_bytes : batch) : 0;
+    gp.nslots = W ? (int)(Wbytes / plan.slot_bytes < (size_t)batch ? Wbytes / plan.slot_bytes : batch) : 0;
     if (gp.nslots < 1) return KMX_ERR_WORKSPACE;
   }
   int rc = device_status_ptr(&gp.status);
@@ -258,18 +319,33 @@ int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* 
   cudaError_t e = ensure_smem(func, dev, smem);
   if (e != cudaSuccess) return KMX_ERR_CUDA;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, 256, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, threads, smem);
   if (per_sm < 1) per_sm = 1;
   long long grid = (long long)di.sms * per_sm;
   if (grid > batch) grid = batch;
   if (!gp.f_in_smem && grid > gp.nslots) grid = gp.nslots;
   void* args[] = {&gp};
-  e = cudaLaunchKernel(func, dim3((unsigned)grid), dim3(256), args, smem, s);
+  e = cudaLaunchKernel(func, dim3((unsigned)grid), dim3(threads), args, smem, s);
   return e == cudaSuccess ? KMX_OK : KMX_ERR_CUDA;
 }
 
 }  // namespace
 }  // namespace kmx
+
+extern "C" size_t kmx_grad_workspace_bytes(int d, int n, int batchCount, int fp64) {
+  if (d < 1 || d > kmx::MAXD || n < 1 || batchCount <= 0) return 0;
+  long long N = 1;
+  for (int i = 0; i < d; ++i) N *= n;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const kmx::DeviceInfo di = kmx::device_info(dev);
+  const kmx::GradPlan g = fp64 ? kmx::grad_plan<double>(d, n, N, di.max_smem_optin)
+                               : kmx::grad_plan<float>(d, n, N, di.max_smem_optin);
+  if (!g.ok || g.f_in_smem) return 0;
+  long long slots = (long long)di.sms * 2;
+  if (slots > batchCount) slots = batchCount;
+  return (size_t)slots * g.slot_bytes;
+}
 
 extern "C" int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
                                              const double* G, double* Y, double* dX, double* dA,

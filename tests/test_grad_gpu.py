@@ -123,5 +123,7 @@ def test_autograd_backward_matches_fused(kmx):
     Y = kronmult(A, X)
     Y.backward(G)
     _, dX, dA = kronmult_fused_grad(A.detach(), X.detach(), G)
-    assert torch.allclose(X.grad, dX, rtol=1e-13, atol=0)
-    assert torch.allclose(A.grad, dA, rtol=1e-13, atol=0)
+    # the Gram reductions use shared-memory atomics: equal up to summation order
+    assert blockwise_rel_err(X.grad.cpu().numpy(), dX.cpu().numpy()) <= 1e-14
+    assert blockwise_rel_err(A.grad.reshape(5, -1).cpu().numpy(),
+                             dA.reshape(5, -1).cpu().numpy()) <= 1e-14
