@@ -62,7 +62,7 @@ def time_one(kmx, torch, d, n, form, engine, target_bytes, reps):
 
 
 def has_tile(d, n):
-    return 3 <= d <= 6 and 2 <= n <= 8
+    return (3 <= d <= 6 and 2 <= n <= 8) or (d == 3 and n == 16)
 
 
 def main(argv=None):
