@@ -396,9 +396,18 @@ template <class Pol, int NN, int D>
 __host__ __device__ constexpr int acc_bytes() {
   return (ipow(NN, D) * (int)sizeof(typename Pol::Out) + 15) / 16 * 16;
 }
+// The X staging block is kept when it fits beside the intermediate; without
+// it, phase 0 reads X straight from HBM (no TMA prefetch).
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr bool stages_x() {
+  return off_stage<Pol, NN, D>() + stage_bytes<Pol, NN, D>() +
+             (buffer_slots<NN, D>() * (int)sizeof(typename Pol::V) + 15) / 16 * 16 +
+             (ipow(NN, D) * (int)sizeof(typename Pol::Out) + 15) / 16 * 16 <=
+         200 * 1024;
+}
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_buf() {
-  return off_stage<Pol, NN, D>() + stage_bytes<Pol, NN, D>();
+  return off_stage<Pol, NN, D>() + (stages_x<Pol, NN, D>() ? stage_bytes<Pol, NN, D>() : 0);
 }
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_acc() {
@@ -533,7 +542,8 @@ tile_kernel(const Problem p) {
   uint32_t uses = 0;  // thread 0: completed phases of the barrier
   auto issue_x = [&](const In* xsrc) {
     int mode = 0;
-    if (xsrc != nullptr && ((reinterpret_cast<uintptr_t>(xsrc) & 15) == 0) && (XBYTES % 16 == 0)) {
+    if (stages_x<Pol, NN, D>() && xsrc != nullptr &&
+        ((reinterpret_cast<uintptr_t>(xsrc) & 15) == 0) && (XBYTES % 16 == 0)) {
       fence_proxy_async();
       mbar_expect_tx(bar, XBYTES);
       tma_load_1d(stage, xsrc, XBYTES, bar);
