@@ -321,51 +321,81 @@ def run_ours(args):
     value = total_flops / (ms * 1e-3) / 1e9
     value_plain = total_flops / (ms_plain * 1e-3) / 1e9
 
-    # e2e through the C ABI from pinned host buffers
+    # e2e through the C ABI from pinned host buffers.  Every step copies its
+    # inputs host->device and its result device->host; steps are pipelined
+    # over two device buffer sets and three streams (inputs in, compute,
+    # result out), so step k's kernel overlaps step k+1's input copies and
+    # step k-1's result copy.
     e2e = None
     if not args.no_e2e:
         Ah = torch.from_numpy(w["Apool"]).pin_memory()
         Xh = torch.from_numpy(w["Xpool"]).pin_memory()
         Yh = torch.zeros_like(Xh).pin_memory()
-        Yout = torch.empty_like(Xh).pin_memory()
         idx_h = torch.from_numpy(np.concatenate(
             [w["y_idx"], w["x_idx"], w["a_idx"].ravel()]).astype(np.int32)).pin_memory()
-        A2, X2, Y2 = torch.empty_like(Ad), torch.empty_like(Xd), torch.empty_like(Xd)
-        idx_d = torch.empty(idx_h.numel(), dtype=torch.int32, device=dev)
+        Yout = [torch.empty_like(Xh).pin_memory() for _ in range(2)]
+        bufs = [dict(A=torch.empty_like(Ad), X=torch.empty_like(Xd), Y=torch.empty_like(Xd),
+                     idx=torch.empty(idx_h.numel(), dtype=torch.int32, device=dev))
+                for _ in range(2)]
         h2d = (Ah.numel() + Xh.numel() + Yh.numel()) * 8 + idx_h.numel() * 4
         d2h = Yh.numel() * 8
+        s_in = [torch.cuda.Stream(), torch.cuda.Stream()]
+        s_cmp = torch.cuda.Stream()
+        s_out = torch.cuda.Stream()
+        ev_in = [torch.cuda.Event() for _ in range(2)]
+        ev_cmp = [torch.cuda.Event() for _ in range(2)]
+        ev_out = [torch.cuda.Event() for _ in range(2)]
+        started = [False, False]
 
-        def e2e_step():
-            A2.copy_(Ah, non_blocking=True)
-            X2.copy_(Xh, non_blocking=True)
-            Y2.copy_(Yh, non_blocking=True)
-            idx_d.copy_(idx_h, non_blocking=True)
-            yi = idx_d[:entries].long()
-            xi = idx_d[entries:2 * entries].long()
-            ai = idx_d[2 * entries:].long().view(entries, D)
-            qA = ((lvl * POOL + ai) * (NN * NN * 8) + A2.data_ptr()).reshape(-1)
-            qX = xi * (N * 8) + X2.data_ptr()
-            qY = yi * (N * 8) + Y2.data_ptr()
-            kmx.kronmult_xbatched(D, NN, qA, NN, qX, qY, None, entries)
-            Yout.copy_(Y2, non_blocking=True)
+        def e2e_step(k):
+            b = k % 2
+            B = bufs[b]
+            if started[b]:  # the previous result copy from this buffer set is done
+                s_in[0].wait_event(ev_out[b])
+                s_in[1].wait_event(ev_out[b])
+            with torch.cuda.stream(s_in[0]):
+                B["X"].copy_(Xh, non_blocking=True)
+                B["idx"].copy_(idx_h, non_blocking=True)
+            with torch.cuda.stream(s_in[1]):
+                B["Y"].copy_(Yh, non_blocking=True)
+                B["A"].copy_(Ah, non_blocking=True)
+            ev_a = torch.cuda.Event()
+            ev_a.record(s_in[1])
+            ev_in[b].record(s_in[0])
+            s_cmp.wait_event(ev_in[b])
+            s_cmp.wait_event(ev_a)
+            with torch.cuda.stream(s_cmp):
+                idx = B["idx"]
+                yi = idx[:entries].long()
+                xi = idx[entries:2 * entries].long()
+                ai = idx[2 * entries:].long().view(entries, D)
+                qA = ((lvl * POOL + ai) * (NN * NN * 8) + B["A"].data_ptr()).reshape(-1)
+                qX = xi * (N * 8) + B["X"].data_ptr()
+                qY = yi * (N * 8) + B["Y"].data_ptr()
+                kmx.kronmult_xbatched(D, NN, qA, NN, qX, qY, None, entries, stream=s_cmp)
+                ev_cmp[b].record(s_cmp)
+            s_out.wait_event(ev_cmp[b])
+            with torch.cuda.stream(s_out):
+                Yout[b].copy_(B["Y"], non_blocking=True)
+                ev_out[b].record(s_out)
+            started[b] = True
 
-        for _ in range(2):
-            e2e_step()
+        for k in range(2):
+            e2e_step(k)
         torch.cuda.synchronize()
-        K2 = max(3, args.steps // 2)
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
+        K2 = max(4, args.steps)
         t0 = time.perf_counter()
-        f0.record(stream)
-        for _ in range(K2):
-            e2e_step()
-        f1.record(stream)
+        for k in range(K2):
+            e2e_step(k)
         torch.cuda.synchronize()
-        wall = (time.perf_counter() - t0) / K2
-        ms_e2e = max(f0.elapsed_time(f1) / K2, wall * 1e3)
+        ms_e2e = (time.perf_counter() - t0) / K2 * 1e3
+        # the last step's result is on the host and correct
+        ok = bool(torch.isfinite(Yout[(K2 - 1) % 2]).all())
         e2e = {"value": round(total_flops / (ms_e2e * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
                "ms_per_step": round(ms_e2e, 3), "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "result_finite": ok,
+               "timing": "host wall clock over K steps, each step = H2D inputs + C ABI call + "
+                         "D2H result; steps pipelined over two buffer sets and copy/compute streams"}
 
     if rank != 0:
         if dist:
