@@ -665,6 +665,62 @@ def run_precision(args):
                       "workload": "precision", "cases": out, "data": "synthetic"}))
 
 
+def run_kgemm(args):
+    """kgemm_{nn,nt}_batched at the reference test's performance shapes
+    (test_kgemm_nn_batched.cpp:541-553: mm = kk = n, nn = n^5) and at the
+    tall-narrow transpose of the same contraction (kgemm_nt with mm = n^5,
+    nn = kk = n), 16384 entries each so that C is larger than L2; alpha 1.3,
+    beta 1.2.  GFLOP/s and the roofline max(flops / FP64-or-FP32 FMA peak,
+    bytes / HBM peak), bytes = A + B + C read + C written."""
+    import ctypes as C
+
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    L = kmx.lib()
+    r64, r32 = C.c_double(0), C.c_double(0)
+    L.kmx_probe_fma_rate(1, C.byref(r64))
+    L.kmx_probe_fma_rate(0, C.byref(r32))
+    hbm = float(load_peaks()[0]["hbm_gbs"]) * 1e9
+    batch = 16384
+    out = []
+    for trans, dt in (("nn", torch.float64), ("nt", torch.float64), ("nn", torch.float32)):
+        for n in (2, 3, 4, 5, 6):
+            big = n ** 5
+            mm, nn, kk = (n, big, n) if trans == "nn" else (big, n, n)
+            esz = 8 if dt == torch.float64 else 4
+            A = torch.randn(batch * mm * kk, dtype=dt, device="cuda")
+            Bm = torch.randn(batch * kk * nn, dtype=dt, device="cuda")
+            Cm = torch.randn(batch * mm * nn, dtype=dt, device="cuda")
+            pA = kmx.pointer_array(A, torch.arange(batch, device="cuda") * (mm * kk))
+            pB = kmx.pointer_array(Bm, torch.arange(batch, device="cuda") * (kk * nn))
+            pC = kmx.pointer_array(Cm, torch.arange(batch, device="cuda") * (mm * nn))
+            ldA = torch.full((batch,), mm, dtype=torch.int32, device="cuda")
+            ldB = torch.full((batch,), kk if trans == "nn" else nn, dtype=torch.int32, device="cuda")
+            fn = kmx.kgemm_nn_batched if trans == "nn" else kmx.kgemm_nt_batched
+            call = lambda: fn(mm, nn, kk, 1.3, pA, ldA, pB, ldB, 1.2, pC, ldA, batch, dtype=dt)
+            ms = _events_time(torch, call, max(3, args.steps), 3)
+            flops = 2.0 * mm * nn * kk * batch
+            nbytes = float(esz) * batch * (mm * kk + kk * nn + 2 * mm * nn)
+            peak = (r64.value if dt == torch.float64 else r32.value) * 2
+            t_roof = max(flops / peak, nbytes / hbm)
+            out.append({"trans": trans, "dtype": "f64" if dt == torch.float64 else "f32",
+                        "mm": mm, "nn": nn, "kk": kk, "batch": batch, "ms": round(ms, 4),
+                        "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
+                        "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                        "bound": "fma" if flops / peak > nbytes / hbm else "hbm",
+                        "roofline_frac": round(t_roof / (ms * 1e-3), 3)})
+            del A, Bm, Cm
+    kmx.check_device_status()
+    fr = [c["roofline_frac"] for c in out]
+    print(json.dumps({"metric": "kgemm batched GFLOP/s and roofline fraction",
+                      "value": round(float(np.exp(np.mean(np.log(fr)))), 3),
+                      "unit": "geomean roofline fraction", "workload": "kgemm",
+                      "fp64_fma_per_s": r64.value, "fp32_fma_per_s": r32.value,
+                      "hbm_gbs": hbm / 1e9, "cases": out, "data": "synthetic"}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -674,7 +730,7 @@ def main():
     ap.add_argument("--entries", type=int, default=ENTRIES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["xbatched", "mixed", "grad", "precision"],
+    ap.add_argument("--workload", choices=["xbatched", "mixed", "grad", "precision", "kgemm"],
                     default="xbatched")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -685,6 +741,8 @@ def main():
         return run_grad(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "kgemm":
+        return run_kgemm(args)
     return run_ours(args)
 
 

@@ -174,6 +174,41 @@ int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aar
                                const kmx_options* opt, kmx_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Stand-alone batched tiny GEMMs (reference kgemm_nn_batched.cpp:8-41,    */
+/* kgemm_nt_batched.cpp:8-41; templates kgemm_nn_batched.hpp:8-81,         */
+/* kgemm_nt_batched.hpp:8-79).                                             */
+/* ---------------------------------------------------------------------- */
+
+/* For each entry e < batchCount, column-major:
+ *   nn: C_e = alpha * A_e * B_e   + beta * C_e,  B_e kk x nn (ldBarray[e] >= kk)
+ *   nt: C_e = alpha * A_e * B_e^T + beta * C_e,  B_e nn x kk (ldBarray[e] >= nn)
+ * with A_e mm x kk (ldAarray[e] >= mm) and C_e mm x nn (ldCarray[e] >= mm).
+ * The pointer arrays and the leading-dimension arrays are device arrays.
+ * beta == 1 adds alpha*A*op(B) into C with atomics, so entries may share one
+ * C; beta == 0 overwrites C; any other beta blends beta*C + alpha*A*op(B)
+ * (entries must not share C), as the reference's epilogue does
+ * (kgemm_nn.hpp:388-400, kgemm_nt.hpp:365-376).  An entry with a NULL
+ * pointer or a leading dimension below its row count is skipped and flagged
+ * in the device status word.  FP32 accumulates in FP32 (the reference
+ * accumulates FP32 data in double). */
+int kmx_kgemm_nn_batched_f64(int mm, int nn, int kk, double alpha, double* const* Aarray,
+                             const int* ldAarray, double* const* Barray, const int* ldBarray,
+                             double beta, double* const* Carray, const int* ldCarray,
+                             int batchCount, kmx_stream_t stream);
+int kmx_kgemm_nt_batched_f64(int mm, int nn, int kk, double alpha, double* const* Aarray,
+                             const int* ldAarray, double* const* Barray, const int* ldBarray,
+                             double beta, double* const* Carray, const int* ldCarray,
+                             int batchCount, kmx_stream_t stream);
+int kmx_kgemm_nn_batched_f32(int mm, int nn, int kk, float alpha, float* const* Aarray,
+                             const int* ldAarray, float* const* Barray, const int* ldBarray,
+                             float beta, float* const* Carray, const int* ldCarray,
+                             int batchCount, kmx_stream_t stream);
+int kmx_kgemm_nt_batched_f32(int mm, int nn, int kk, float alpha, float* const* Aarray,
+                             const int* ldAarray, float* const* Barray, const int* ldBarray,
+                             float beta, float* const* Carray, const int* ldCarray,
+                             int batchCount, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Differentiation (no counterpart in the reference, which has no backward).  */
 /* ---------------------------------------------------------------------- */
 

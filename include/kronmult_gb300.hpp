@@ -66,6 +66,40 @@ KMX_DROPIN_SQUARE(5)
 KMX_DROPIN_SQUARE(6)
 #undef KMX_DROPIN_SQUARE
 
+// kgemm_{nn,nt}_batched (kgemm_nn_batched.cpp:8-41, kgemm_nt_batched.cpp:8-41)
+inline void kgemm_nn_batched(int const mm, int const nn, int const kk, double const alpha,
+                             double* const Aarray_[], int const ldAarray_[],
+                             double* const Barray_[], int const ldBarray_[], double const beta,
+                             double* const Carray_[], int const ldCarray_[],
+                             int const batchCount) {
+  kmx_detail::check(kmx_kgemm_nn_batched_f64(mm, nn, kk, alpha, Aarray_, ldAarray_, Barray_,
+                                             ldBarray_, beta, Carray_, ldCarray_, batchCount, 0));
+}
+inline void kgemm_nt_batched(int const mm, int const nn, int const kk, double const alpha,
+                             double* const Aarray_[], int const ldAarray_[],
+                             double* const Barray_[], int const ldBarray_[], double const beta,
+                             double* const Carray_[], int const ldCarray_[],
+                             int const batchCount) {
+  kmx_detail::check(kmx_kgemm_nt_batched_f64(mm, nn, kk, alpha, Aarray_, ldAarray_, Barray_,
+                                             ldBarray_, beta, Carray_, ldCarray_, batchCount, 0));
+}
+inline void kgemm_nn_batched(int const mm, int const nn, int const kk, float const alpha,
+                             float* const Aarray_[], int const ldAarray_[],
+                             float* const Barray_[], int const ldBarray_[], float const beta,
+                             float* const Carray_[], int const ldCarray_[],
+                             int const batchCount) {
+  kmx_detail::check(kmx_kgemm_nn_batched_f32(mm, nn, kk, alpha, Aarray_, ldAarray_, Barray_,
+                                             ldBarray_, beta, Carray_, ldCarray_, batchCount, 0));
+}
+inline void kgemm_nt_batched(int const mm, int const nn, int const kk, float const alpha,
+                             float* const Aarray_[], int const ldAarray_[],
+                             float* const Barray_[], int const ldBarray_[], float const beta,
+                             float* const Carray_[], int const ldCarray_[],
+                             int const batchCount) {
+  kmx_detail::check(kmx_kgemm_nt_batched_f32(mm, nn, kk, alpha, Aarray_, ldAarray_, Barray_,
+                                             ldBarray_, beta, Carray_, ldCarray_, batchCount, 0));
+}
+
 // vbatched: (m1,n1, ..., md,nd, Aarray, pX, pY, W, Wcapacity_bytes, batchCount)
 template <typename T>
 inline int kmx_vbatched_dispatch(int d, const int* m, const int* n, T const* const Aarray_[],

@@ -156,6 +156,34 @@ def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subba
     check(rc, f"kronmult{d}_xbatched")
 
 
+def _kgemm(trans, mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
+           batchCount, dtype, stream):
+    t = _torch()
+    f64 = _is_f64(dtype if dtype is not None else t.float64)
+    b = batchCount if batchCount is not None else Carray.numel()
+    fn = getattr(lib(), f"kmx_kgemm_{trans}_batched_{'f64' if f64 else 'f32'}")
+    rc = fn(mm, nn, kk, float(alpha), _addr(Aarray), _addr(ldAarray), _addr(Barray),
+            _addr(ldBarray), float(beta), _addr(Carray), _addr(ldCarray), b,
+            C.c_void_p(_stream(stream)))
+    check(rc, f"kgemm_{trans}_batched")
+
+
+def kgemm_nn_batched(mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
+                     batchCount=None, *, dtype=None, stream=None):
+    """kgemm_nn_batched (kgemm_nn_batched.cpp:8-41): C_e = alpha*A_e*B_e + beta*C_e
+    for every entry; pointer arrays (int64 device tensors of addresses) and
+    int32 leading-dimension arrays live on the device."""
+    _kgemm("nn", mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
+           batchCount, dtype, stream)
+
+
+def kgemm_nt_batched(mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
+                     batchCount=None, *, dtype=None, stream=None):
+    """kgemm_nt_batched (kgemm_nt_batched.cpp:8-41): C_e = alpha*A_e*B_e^T + beta*C_e."""
+    _kgemm("nt", mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
+           batchCount, dtype, stream)
+
+
 def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, batchCount=None, *,
                       dtype=None, form=None, accumulate=None, transpose=False, engine=None,
                       stream=None):

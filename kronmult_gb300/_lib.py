@@ -80,6 +80,14 @@ _SIGS = {
     "kmx_kronmult_batched_grad_f32": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp],
     "kmx_kronmult_xbatched_wide": [_i, _i, _i, _vp, _i, _vp, _vp, _i, _optp, _vp],
     "kmx_kronmult_mixed_f64": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
+    "kmx_kgemm_nn_batched_f64": [_i, _i, _i, C.c_double, _vp, _vp, _vp, _vp, C.c_double, _vp, _vp,
+                                 _i, _vp],
+    "kmx_kgemm_nt_batched_f64": [_i, _i, _i, C.c_double, _vp, _vp, _vp, _vp, C.c_double, _vp, _vp,
+                                 _i, _vp],
+    "kmx_kgemm_nn_batched_f32": [_i, _i, _i, C.c_float, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp,
+                                 _i, _vp],
+    "kmx_kgemm_nt_batched_f32": [_i, _i, _i, C.c_float, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp,
+                                 _i, _vp],
     "kmx_kronmult_mixed_f32": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
     "kmx_set_default_options": [_optp],
     "kmx_get_default_options": [_optp],

@@ -344,3 +344,59 @@ double kmo_kron_flops(int d, const int* m, const int* n) {
   double f1 = 2.0 * rest * n[0] * m[0];
   return f1 + kmo_kron_flops(d - 1, m + 1, n + 1) * m[0];
 }
+
+/* ------------------------------------------------------------------ */
+/* Stand-alone batched tiny GEMMs: kgemm_nn_batched / kgemm_nt_batched */
+/* ------------------------------------------------------------------ */
+
+/* Entry ib: C = alpha * A * op(B) + beta * C, A mm x kk, C mm x nn,
+ * op(B) = B (kk x nn) for "nn", transpose(B) with B nn x kk for "nt".
+ * Follows kgemm_nn_batched.hpp:8-81 / kgemm_nt_batched.hpp:8-79 (one entry
+ * after another) and the per-element epilogue of kgemm_nn_v1
+ * (kgemm_nn.hpp:388-400) / kgemm_nt_v1 (kgemm_nt.hpp:365-376):
+ *   beta == 1: C += alpha*c with an atomic update (entries may share C);
+ *   beta == 0: C  = alpha*c;
+ *   otherwise: C  = beta*C + alpha*c.
+ * The nn epilogue rounds alpha*c to T before it is used (kgemm_nn.hpp:390);
+ * the nt epilogue blends beta*C + alpha*c in the accumulation type and
+ * rounds once (kgemm_nt.hpp:375).  For FP64 the two are the same.
+ * The dot product c starts from zero and runs over k in increasing order.
+ * FP32 follows the reference's float specialisation (kgemm_nn.hpp:688-701,
+ * kgemm_nt.hpp:557-571): accumulate, scale and blend in double, round when
+ * stored. */
+#define DEFINE_KGEMM(NAME, T, TRANSB)                                                     \
+  void NAME(int mm, int nn, int kk, T alpha, const T* const* Aarray, const int* ldAarray, \
+            const T* const* Barray, const int* ldBarray, T beta, T* const* Carray,        \
+            const int* ldCarray, int batch) {                                             \
+    const double al = (double)alpha, be = (double)beta;                                   \
+    _Pragma("omp parallel for schedule(dynamic, 1)")                                      \
+    for (int ib = 0; ib < batch; ++ib) {                                                  \
+      const T* A = Aarray[ib];                                                            \
+      const T* B = Barray[ib];                                                            \
+      T* C = Carray[ib];                                                                  \
+      const size_t ldA = (size_t)ldAarray[ib], ldB = (size_t)ldBarray[ib];                \
+      const size_t ldC = (size_t)ldCarray[ib];                                            \
+      for (int j = 0; j < nn; ++j)                                                        \
+        for (int i = 0; i < mm; ++i) {                                                    \
+          double c = 0;                                                                   \
+          for (int k = 0; k < kk; ++k) {                                                  \
+            const double b = TRANSB ? (double)B[j + k * ldB] : (double)B[k + j * ldB];    \
+            c += (double)A[i + k * ldA] * b;                                              \
+          }                                                                               \
+          T* p = &C[i + j * ldC];                                                         \
+          const T ac = (T)(al * c);                                                       \
+          if (be == 1.0) {                                                                \
+            _Pragma("omp atomic update") *p += ac;                                        \
+          } else if (be == 0.0) {                                                         \
+            *p = ac;                                                                      \
+          } else {                                                                        \
+            *p = TRANSB ? (T)(be * (double)*p + al * c) : (T)(be * (double)*p + (double)ac); \
+          }                                                                               \
+        }                                                                                 \
+    }                                                                                     \
+  }
+
+DEFINE_KGEMM(kmo_kgemm_nn_batched_f64, double, 0)
+DEFINE_KGEMM(kmo_kgemm_nt_batched_f64, double, 1)
+DEFINE_KGEMM(kmo_kgemm_nn_batched_f32, float, 0)
+DEFINE_KGEMM(kmo_kgemm_nt_batched_f32, float, 1)

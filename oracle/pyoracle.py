@@ -232,3 +232,38 @@ def ramp_a(n, d, batch, lda=None, dtype=np.float64):
             r1 = i[None, :] + (j[:, None] - 1) * n + l * n * n + kb * batch
             out[kb, l, :, :n] = r1 / (n * n * d * batch)
     return out.astype(dtype)
+
+
+def kgemm_batched(trans, mm, nn, kk, alpha, Abuf, aoff, ldA, Bbuf, boff, ldB, beta, Cbuf, coff,
+                  ldC, lib=None):
+    """kgemm_nn_batched / kgemm_nt_batched (kgemm_nn_batched.hpp:8-81,
+    kgemm_nt_batched.hpp:8-79): for each entry, C = alpha*A*op(B) + beta*C.
+    trans is "nn" or "nt"; *off are element offsets of each entry's matrix in
+    its buffer; ldA/ldB/ldC are per-entry leading dimensions."""
+    s = _suffix(Abuf.dtype)
+    batch = len(aoff)
+    pA, pB, pC = _ptr_array(Abuf, aoff), _ptr_array(Bbuf, boff), _ptr_array(Cbuf, coff)
+    sc = C.c_double if s == "f64" else C.c_float
+    args = (C.c_int(mm), C.c_int(nn), C.c_int(kk), sc(alpha), pA, _ints(ldA), pB, _ints(ldB),
+            sc(beta), pC, _ints(ldC), C.c_int(batch))
+    if lib == "ref":
+        assert getattr(ref_lib(), f"ref_kgemm_{trans}_batched_{s}")(*args) == 0
+    else:
+        getattr(oracle_lib(), f"kmo_kgemm_{trans}_batched_{s}")(*args)
+
+
+def ramp_kgemm(trans, mm, nn, kk, batch, dtype=np.float64):
+    """The closed-form inputs of test_kgemm_nn_batched.cpp:181-217 (and the nt
+    test): A(i,j) = 1+i+j*nrowA+ib, B(i,j) = 1/(1+i+j*nrowB+ib), C = 1, with
+    1-based i, j and ld = number of rows.  Returns (A, B, C) as
+    (batch, rows*cols) column-major arrays."""
+    nrowB, ncolB = (kk, nn) if trans == "nn" else (nn, kk)
+    A = np.empty((batch, mm * kk), dtype=np.float64)
+    B = np.empty((batch, nrowB * ncolB), dtype=np.float64)
+    for ib in range(batch):
+        i, j = np.meshgrid(np.arange(1, mm + 1), np.arange(1, kk + 1), indexing="ij")
+        A[ib] = (1.0 + i + j * mm + ib).ravel(order="F")
+        i, j = np.meshgrid(np.arange(1, nrowB + 1), np.arange(1, ncolB + 1), indexing="ij")
+        B[ib] = (1.0 / (1.0 + i + j * nrowB + ib)).ravel(order="F")
+    Cm = np.ones((batch, mm * nn), dtype=np.float64)
+    return A.astype(dtype), B.astype(dtype), Cm.astype(dtype)

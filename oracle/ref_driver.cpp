@@ -9,6 +9,8 @@
 //   kronmult{d}_pbatched<T>  kronmult6_pbatched.hpp:14-81
 //   kronmult{d}_xbatched<T>  kronmult6_xbatched.hpp:14-46 -> kronmult_xbatched.hpp:19-157
 //   kronmult{d}_vbatched<T>  kronmult6_vbatched.hpp:14-58 -> kronmult_vbatched.hpp:19-248
+//   kgemm_nn_batched<T>      kgemm_nn_batched.hpp:8-81
+//   kgemm_nt_batched<T>      kgemm_nt_batched.hpp:8-79
 #include <cstddef>
 #include "kronmult1_batched.hpp"
 #include "kronmult2_batched.hpp"
@@ -34,6 +36,8 @@
 #include "kronmult4_vbatched.hpp"
 #include "kronmult5_vbatched.hpp"
 #include "kronmult6_vbatched.hpp"
+#include "kgemm_nn_batched.hpp"
+#include "kgemm_nt_batched.hpp"
 
 template <typename T>
 static int batched(int d, int n, const T* A, T* X, T* Y, T* W, int b) {
@@ -97,4 +101,9 @@ int ref_xbatched_f64(int d, int n, const double* const* A, int lda, double** X, 
 int ref_xbatched_f32(int d, int n, const float* const* A, int lda, float** X, float** Y, float** W, int b, int sub) { return xbatched<float>(d, n, A, lda, X, Y, W, b, sub); }
 int ref_vbatched_f64(int d, const int* m, const int* n, const double* const* A, double** X, double** Y, double* W, size_t cap, int b) { return vbatched<double>(d, m, n, A, X, Y, W, cap, b); }
 int ref_vbatched_f32(int d, const int* m, const int* n, const float* const* A, float** X, float** Y, float* W, size_t cap, int b) { return vbatched<float>(d, m, n, A, X, Y, W, cap, b); }
+
+int ref_kgemm_nn_batched_f64(int mm, int nn, int kk, double alpha, double* const* A, const int* ldA, double* const* B, const int* ldB, double beta, double* const* C, const int* ldC, int b) { kgemm_nn_batched<double>(mm, nn, kk, alpha, A, ldA, B, ldB, beta, C, ldC, b); return 0; }
+int ref_kgemm_nt_batched_f64(int mm, int nn, int kk, double alpha, double* const* A, const int* ldA, double* const* B, const int* ldB, double beta, double* const* C, const int* ldC, int b) { kgemm_nt_batched<double>(mm, nn, kk, alpha, A, ldA, B, ldB, beta, C, ldC, b); return 0; }
+int ref_kgemm_nn_batched_f32(int mm, int nn, int kk, float alpha, float* const* A, const int* ldA, float* const* B, const int* ldB, float beta, float* const* C, const int* ldC, int b) { kgemm_nn_batched<float>(mm, nn, kk, alpha, A, ldA, B, ldB, beta, C, ldC, b); return 0; }
+int ref_kgemm_nt_batched_f32(int mm, int nn, int kk, float alpha, float* const* A, const int* ldA, float* const* B, const int* ldB, float beta, float* const* C, const int* ldC, int b) { kgemm_nt_batched<float>(mm, nn, kk, alpha, A, ldA, B, ldB, beta, C, ldC, b); return 0; }
 }

@@ -83,7 +83,7 @@ def test_default_options_roundtrip(kmx):
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
 def test_cpp_dropin_header_compiles_and_links(kmx, tmp_path):
     """A translation unit written against the reference's host API (names,
-    argument order, default subbatchCount) builds against our header and
+    argument order, default subbatchCount, the kgemm batched API) builds against our header and
     library without edits."""
     src = tmp_path / "user.cpp"
     src.write_text(r'''
@@ -97,6 +97,9 @@ void user(int n, double* A, double** pA, double** pX, double** pY, double** pW, 
   kronmult3_xbatched(n, pAf, n, pXf, pYf, pWf, batch, 8);
   kronmult2_vbatched<double>(2, 3, 4, 5, pA, pX, pY, W, 1 << 20, batch);
   kronmult6_vbatched<float>(1, 2, 2, 1, 1, 1, 2, 2, 3, 3, 2, 2, pAf, pXf, pYf, Af, 1 << 20, batch);
+  int* ld = nullptr;
+  kgemm_nn_batched(4, 1024, 4, 1.3, pA, ld, pX, ld, 1.2, pY, ld, batch);
+  kgemm_nt_batched(1024, 4, 4, 1.0, pXf, ld, pAf, ld, 0.0f, pWf, ld, batch);
 }
 int main() { return 0; }
 ''')
@@ -106,3 +109,16 @@ int main() { return 0; }
                     str(src), "-o", str(exe), f"-L{lib_dir}", "-lkronmult_gb300",
                     f"-Wl,-rpath,{lib_dir}"], check=True)
     assert exe.exists()
+
+
+def test_kgemm_argument_checks_without_gpu(kmx):
+    L = kmx.lib()
+    for fn in (L.kmx_kgemm_nn_batched_f64, L.kmx_kgemm_nt_batched_f64,
+               L.kmx_kgemm_nn_batched_f32, L.kmx_kgemm_nt_batched_f32):
+        assert fn(-1, 4, 4, 1.0, 8, 8, 8, 8, 0.0, 8, 8, 2, None) == 1  # negative size
+        assert fn(4, 4, 4, 1.0, 8, 8, 8, 8, 0.0, 8, 8, -1, None) == 1  # negative batch
+        assert fn(4, 4, 4, 1.0, 8, 8, 8, 8, 0.0, 0, 8, 2, None) == 2   # no C array
+        assert fn(4, 4, 4, 1.0, 0, 8, 8, 8, 0.0, 8, 8, 2, None) == 2   # no A array with kk > 0
+        assert fn(4, 4, 4, 1.0, 8, 8, 8, 0, 0.0, 8, 8, 2, None) == 2   # no ldB array
+        assert fn(4, 4, 4, 1.0, 0, 0, 0, 0, 0.0, 0, 0, 0, None) == 0   # empty batch
+        assert fn(0, 4, 4, 1.0, 0, 0, 0, 0, 0.0, 0, 0, 3, None) == 0   # empty matrices

@@ -1,5 +1,7 @@
 """CPU tests of the oracle: pinned against the golden vectors produced by the
 reference's own CPU build, and against an explicit-Kronecker evaluation."""
+import os
+
 import numpy as np
 import pytest
 
@@ -147,3 +149,66 @@ def test_planted_mistake_is_caught(po1):
     Y = np.zeros_like(X)
     po1.batched(d, n, A, X.copy(), Y, np.zeros_like(X), batch)
     assert not np.array_equal(Y, g[f"batched_d{d}_n{n}_b{batch}"])
+
+
+# ---------------------------------------------------------------------------
+# kgemm_{nn,nt}_batched
+# ---------------------------------------------------------------------------
+
+def _kgemm_cases():
+    from tests.golden import make_kgemm_golden as mk
+
+    for trans in ("nn", "nt"):
+        for tag in ("f64", "f32"):
+            for shape in mk.SHAPES:
+                for bname, beta in mk.BETAS:
+                    if bname != "b12" and shape not in mk.ALL_BETAS:
+                        continue
+                    yield trans, tag, shape, bname, beta
+
+
+def test_kgemm_oracle_matches_golden_bitwise(po1):
+    from tests.golden import make_kgemm_golden as mk
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "kgemm_golden.npz"))
+    n = 0
+    for trans, tag, (mm, nn, kk, batch), bname, beta in _kgemm_cases():
+        T = np.float64 if tag == "f64" else np.float32
+        got = mk.run(trans, T, mm, nn, kk, batch, beta, lib=None)
+        ref = g[mk.case_key(trans, tag, mm, nn, kk, batch, bname)]
+        assert got.dtype == ref.dtype and np.array_equal(got, ref), (trans, tag, mm, nn, kk, bname)
+        n += 1
+    for trans in ("nn", "nt"):
+        for tag, T in (("f64", np.float64), ("f32", np.float32)):
+            got = mk.run(trans, T, 8, 15, 22, 8, 1.0, shared_c=True, lib=None)
+            assert np.array_equal(got, g[f"{trans}_{tag}_shared_8x15x22_b8"])
+    assert n == 56
+
+
+@pytest.mark.parametrize("trans", ["nn", "nt"])
+def test_kgemm_oracle_closed_form_sweep(oracle, trans):
+    """The reference test's own check (test_kgemm_nn_batched.cpp:458-487,
+    main_func :525-560): C = alpha*A*op(B) + beta*1 against a direct sum,
+    max abs error below 1e-9 (FP64) / 5e-4 (FP32), alpha 1.3, beta 1.2, over
+    mm, nn, kk in 1..65 step 7 (every other step here) and batch 1, 8, 15."""
+    for T, tol in ((np.float64, 1e-9), (np.float32, 5e-4)):
+        for batch in (1, 8, 15):
+            for kk in range(1, 66, 14):
+                for nn in range(1, 66, 14):
+                    for mm in range(1, 66, 14):
+                        A, B, Cm = oracle.ramp_kgemm(trans, mm, nn, kk, batch, dtype=T)
+                        C = Cm.copy()
+                        ldb = kk if trans == "nn" else nn
+                        oracle.kgemm_batched(trans, mm, nn, kk, 1.3, A.reshape(-1),
+                                             [i * mm * kk for i in range(batch)], [mm] * batch,
+                                             B.reshape(-1), [i * B.shape[1] for i in range(batch)],
+                                             [ldb] * batch, 1.2, C.reshape(-1),
+                                             [i * mm * nn for i in range(batch)], [mm] * batch)
+                        Ad = A.astype(np.float64).reshape(batch, kk, mm).transpose(0, 2, 1)
+                        Bd = B.astype(np.float64)
+                        # op(B) indexed [b, k, j]: B is kk x nn (nn) or nn x kk (nt), column-major
+                        Bm = (Bd.reshape(batch, nn, kk).transpose(0, 2, 1) if trans == "nn"
+                              else Bd.reshape(batch, kk, nn))
+                        exact = 1.3 * np.einsum("bik,bkj->bij", Ad, Bm) + 1.2
+                        got = C.astype(np.float64).reshape(batch, nn, mm).transpose(0, 2, 1)
+                        assert np.abs(got - exact).max() < tol, (T, batch, mm, nn, kk)
