@@ -189,8 +189,9 @@ int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aar
  * (entries must not share C), as the reference's epilogue does
  * (kgemm_nn.hpp:388-400, kgemm_nt.hpp:365-376).  An entry with a NULL
  * pointer or a leading dimension below its row count is skipped and flagged
- * in the device status word.  FP32 accumulates in FP32 (the reference
- * accumulates FP32 data in double). */
+ * in the device status word.  FP32 keeps each dot product as a pair of FP32
+ * values (exact products, exact two-sums: about 48 bits) and rounds once when
+ * stored, like the reference's accumulation of FP32 data in double. */
 int kmx_kgemm_nn_batched_f64(int mm, int nn, int kk, double alpha, double* const* Aarray,
                              const int* ldAarray, double* const* Barray, const int* ldBarray,
                              double beta, double* const* Carray, const int* ldCarray,

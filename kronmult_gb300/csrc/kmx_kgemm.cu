@@ -41,6 +41,68 @@ struct KgArgs {
   int* status;
 };
 
+// Dot-product accumulator.  FP64: one FP64 fused multiply-add per term.
+// FP32: the reference accumulates FP32 data in double (kgemm_nn.hpp:688-701,
+// kgemm_nt.hpp:557-571); here the sum is kept as an unevaluated pair of FP32
+// values (s + c) with exact products (FMA residual) and an exact two-sum per
+// term, about 48 bits, so the stored result carries one rounding to FP32 as
+// in the reference, without using the FP64 pipe.
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+  double s;
+  __device__ __forceinline__ void zero() { s = 0.0; }
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  template <bool TRANS_B>
+  __device__ __forceinline__ void store(double* p, double alpha, double beta) const {
+    const double v = alpha * s;  // kgemm_nn.hpp:390 / kgemm_nt.hpp:368
+    if (beta == 1.0) {
+      atomicAdd(p, v);
+    } else if (beta == 0.0) {
+      *p = v;
+    } else {
+      *p = fma(beta, *p, v);
+    }
+  }
+};
+
+template <>
+struct Acc<float> {
+  float s, c;
+  __device__ __forceinline__ void zero() { s = c = 0.f; }
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+  }
+  template <bool TRANS_B>
+  __device__ __forceinline__ void store(float* p, float alpha, float beta) const {
+    // renormalise (t, l) = s + c, then alpha*(t + l) with one rounding
+    const float t = __fadd_rn(s, c);
+    const float l = __fsub_rn(c, __fsub_rn(t, s));
+    const float al = __fmul_rn(alpha, l);
+    if (beta == 1.f) {
+      atomicAdd(p, __fmaf_rn(alpha, t, al));
+    } else if (beta == 0.f) {
+      *p = __fmaf_rn(alpha, t, al);
+    } else if (TRANS_B) {
+      // nt blends beta*C + alpha*c before rounding (kgemm_nt.hpp:375)
+      const float bc = __fmul_rn(beta, *p);
+      const float be = __fmaf_rn(beta, *p, -bc);
+      *p = __fadd_rn(__fmaf_rn(alpha, t, bc), __fadd_rn(al, be));
+    } else {
+      // nn rounds alpha*c first, then blends (kgemm_nn.hpp:390-399)
+      *p = __fmaf_rn(beta, *p, __fmaf_rn(alpha, t, al));
+    }
+  }
+};
+
 constexpr int KG_THREADS = 256;
 constexpr int KG_BK = 16;
 
@@ -74,11 +136,11 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_kernel(KgArgs<T> a) {
       if (tid == 0) atomicOr(a.status, DF_BAD_SHAPE);
       continue;
     }
-    T acc[TM][TN];
+    Acc<T> acc[TM][TN];
 #pragma unroll
     for (int r = 0; r < TM; ++r)
 #pragma unroll
-      for (int c = 0; c < TN; ++c) acc[r][c] = T(0);
+      for (int c = 0; c < TN; ++c) acc[r][c].zero();
 
     for (int k0 = 0; k0 < a.kk; k0 += KG_BK) {
       const int kc = min(KG_BK, a.kk - k0);
@@ -111,10 +173,9 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_kernel(KgArgs<T> a) {
 #pragma unroll
         for (int r = 0; r < TM; ++r)
 #pragma unroll
-          for (int c = 0; c < TN; ++c) acc[r][c] = fma(av[r], bv[c], acc[r][c]);
+          for (int c = 0; c < TN; ++c) acc[r][c].add(av[r], bv[c]);
       }
     }
-    const T alpha = a.alpha, beta = a.beta;
 #pragma unroll
     for (int c = 0; c < TN; ++c) {
       const int j = n0 + tc + c * CT;
@@ -123,15 +184,7 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_kernel(KgArgs<T> a) {
       for (int r = 0; r < TM; ++r) {
         const int i = m0 + tr + r * RT;
         if (i >= a.mm) continue;
-        T* p = Cp + i + j * ldc;
-        const T v = alpha * acc[r][c];
-        if (beta == T(1)) {
-          atomicAdd(p, v);
-        } else if (beta == T(0)) {
-          *p = v;
-        } else {
-          *p = fma(beta, *p, v);
-        }
+        acc[r][c].template store<TRANS_B>(Cp + i + j * ldc, a.alpha, a.beta);
       }
     }
   }
