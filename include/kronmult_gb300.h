@@ -43,12 +43,19 @@ typedef enum kmx_status {
                                 through the device status word, bit 16) */
 } kmx_status;
 
-/* Arithmetic form of the FP64 entry points. */
+/* Arithmetic form.  FP64 entry points: AUTO, PLAIN, SPLIT.  FP32-stored
+ * entry points (the _f32 functions and kmx_kronmult_xbatched_wide): FP32
+ * fused multiply-add unless TF32X3 is asked for. */
 typedef enum kmx_form {
   KMX_FORM_AUTO = 0,   /* per-(d,n) choice from the tuning table */
   KMX_FORM_PLAIN = 1,  /* native FP64 fused multiply-add */
-  KMX_FORM_SPLIT = 2   /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
+  KMX_FORM_SPLIT = 2,  /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
                           ~2^-47 relative per operation, FP64 in and out */
+  KMX_FORM_TF32X3 = 3  /* FP32-stored data only: tensor cores (mma.sync TF32), each
+                          operand split into two TF32 parts, three products, FP32
+                          accumulation (~2^-21 relative per product).  Square n = 4
+                          (d = 4, 6), n = 8 (d = 3..5), n = 16 (d = 2, 3), atomic mode;
+                          other shapes and the deterministic mode use FP32 FMA. */
 } kmx_form;
 
 /* How contributions of entries that share a Y block are combined. */
@@ -172,6 +179,40 @@ typedef enum kmx_in_type {
 int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aarray, int lda,
                                const void* const* pX, double* const* pY, int batchCount,
                                const kmx_options* opt, kmx_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Construction of the xbatched arrays from index triples (no counterpart  */
+/* in the reference, whose tests build them on the host,                   */
+/* test_kronmult6_xbatched.cpp:253-321).                                   */
+/* ---------------------------------------------------------------------- */
+
+/* Writes, for each entry e < count, the kmx_kronmult_xbatched_* arrays
+ *   pY[e]           = Ypool + y_idx[e] * y_stride
+ *   pX[e]           = Xpool + x_idx[e] * x_stride
+ *   Aarray[e*d + l] = Apool + l * a_level_stride + a_idx[e*d + l] * a_pool_stride
+ * (strides in elements; y_idx, x_idx, a_idx are int32 device arrays; the
+ * outputs are device arrays of count, count and d*count pointers).  An index
+ * outside [0, n_y), [0, n_x) or [0, n_pool) yields a NULL pointer and sets
+ * the device status word.  With sort_by_y nonzero the entries are first
+ * ordered by y_idx (stable, on the device), which keeps the atomic updates of
+ * one Y block close together in time; this needs a device workspace of
+ * kmx_xbatched_build_workspace_bytes(count) bytes.  Asynchronous, no host
+ * synchronisation. */
+size_t kmx_xbatched_build_workspace_bytes(int count);
+int kmx_xbatched_build_f64(int d, const double* Apool, long long a_level_stride,
+                           long long a_pool_stride, int n_pool, const double* Xpool,
+                           long long x_stride, int n_x, double* Ypool, long long y_stride, int n_y,
+                           const int* y_idx, const int* x_idx, const int* a_idx, int count,
+                           int sort_by_y, void* workspace, size_t workspace_bytes,
+                           const double** Aarray, const double** pX, double** pY,
+                           kmx_stream_t stream);
+int kmx_xbatched_build_f32(int d, const float* Apool, long long a_level_stride,
+                           long long a_pool_stride, int n_pool, const float* Xpool,
+                           long long x_stride, int n_x, float* Ypool, long long y_stride, int n_y,
+                           const int* y_idx, const int* x_idx, const int* a_idx, int count,
+                           int sort_by_y, void* workspace, size_t workspace_bytes,
+                           const float** Aarray, const float** pX, float** pY,
+                           kmx_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Stand-alone batched tiny GEMMs (reference kgemm_nn_batched.cpp:8-41,    */

@@ -115,7 +115,7 @@ def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accum
         if form not in (None, "auto", "plain"):
             raise KmxError(4, "kmx_kronmult_batched_f32")
         rc = L.kmx_kronmult_batched_f32_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
-                                           _opt(None, accumulate, transpose, engine), s)
+                                           _opt(form, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_batched")
 
 
@@ -131,7 +131,7 @@ def kronmult_pbatched(d, n, A, pX, pY, pW=None, batchCount=None, *, form=None, a
                                             _opt(form, accumulate, transpose, engine), s)
     else:
         rc = L.kmx_kronmult_pbatched_f32_ex(d, n, _addr(A), _addr(pX), _addr(pY), _addr(pW), b,
-                                            _opt(None, accumulate, transpose, engine), s)
+                                            _opt(form, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_pbatched")
 
 
@@ -152,8 +152,39 @@ def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subba
     else:
         rc = L.kmx_kronmult_xbatched_f32_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
                                             _addr(pW), b, subbatchCount,
-                                            _opt(None, accumulate, transpose, engine), s)
+                                            _opt(form, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_xbatched")
+
+
+def xbatched_build(d, Apool, a_level_stride, a_pool_stride, n_pool, Xpool, x_stride, n_x, Ypool,
+                   y_stride, n_y, y_idx, x_idx, a_idx, *, sort_by_y=False, workspace=None,
+                   stream=None):
+    """Device-side construction of the xbatched arrays from index triples.
+
+    Apool/Xpool/Ypool are CUDA tensors (float64 or float32); strides are in
+    elements; y_idx, x_idx (count,) and a_idx (count, d) are int32 CUDA
+    tensors.  Returns (Aarray, pX, pY) as int64 CUDA tensors of addresses
+    (d*count, count, count), entries ordered by y when sort_by_y."""
+    t = _torch()
+    count = int(y_idx.numel())
+    f64 = _is_f64(Xpool.dtype)
+    dev = Xpool.device
+    pA = t.empty(d * count, dtype=t.int64, device=dev)
+    pX = t.empty(count, dtype=t.int64, device=dev)
+    pY = t.empty(count, dtype=t.int64, device=dev)
+    ws_bytes = 0
+    if sort_by_y and workspace is None:
+        ws_bytes = int(lib().kmx_xbatched_build_workspace_bytes(count))
+        workspace = t.empty(ws_bytes, dtype=t.uint8, device=dev)
+    elif workspace is not None:
+        ws_bytes = workspace.numel() * workspace.element_size()
+    fn = lib().kmx_xbatched_build_f64 if f64 else lib().kmx_xbatched_build_f32
+    rc = fn(d, _addr(Apool), int(a_level_stride), int(a_pool_stride), int(n_pool), _addr(Xpool),
+            int(x_stride), int(n_x), _addr(Ypool), int(y_stride), int(n_y), _addr(y_idx),
+            _addr(x_idx), _addr(a_idx), count, 1 if sort_by_y else 0, _addr(workspace), ws_bytes,
+            _addr(pA), _addr(pX), _addr(pY), C.c_void_p(_stream(stream)))
+    check(rc, "xbatched_build")
+    return pA, pX, pY
 
 
 def _kgemm(trans, mm, nn, kk, alpha, Aarray, ldAarray, Barray, ldBarray, beta, Carray, ldCarray,
@@ -202,18 +233,18 @@ def kronmult_vbatched(d, m, n, Aarray, pX, pY, W=None, Wcapacity_bytes=None, bat
                                             _addr(W), cap, b, _opt(form, accumulate, transpose, engine), s)
     else:
         rc = L.kmx_kronmult_vbatched_f32_ex(d, mm, nn, _addr(Aarray), _addr(pX), _addr(pY),
-                                            _addr(W), cap, b, _opt(None, accumulate, transpose, engine), s)
+                                            _addr(W), cap, b, _opt(form, accumulate, transpose, engine), s)
     check(rc, f"kronmult{d}_vbatched")
 
 
 def kronmult_xbatched_wide(d, n, Aarray, lda, pX, pY, batchCount=None, *, in_dtype="f32",
-                           accumulate=None, engine=None, stream=None):
+                           form=None, accumulate=None, engine=None, stream=None):
     """xbatched with FP32 ("f32") or bfloat16 ("bf16") X and factors, FP32
-    arithmetic and FP64 Y accumulation."""
+    arithmetic (form "tf32x3": tensor cores) and FP64 Y accumulation."""
     code = {"f32": 1, "bf16": 2}[in_dtype]
     b = batchCount if batchCount is not None else pX.numel()
     rc = lib().kmx_kronmult_xbatched_wide(code, d, n, _addr(Aarray), lda, _addr(pX), _addr(pY), b,
-                                          _opt(None, accumulate, False, engine),
+                                          _opt(form, accumulate, False, engine),
                                           C.c_void_p(_stream(stream)))
     check(rc, f"kronmult{d}_xbatched_wide")
 

@@ -27,7 +27,7 @@ STATUS = {
     7: "KMX_ERR_OVERLAP",
 }
 
-FORMS = {"auto": 0, "plain": 1, "split": 2}
+FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3}
 ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2}
 ACCUMULATE = {"atomic": 0, "deterministic": 1}
 
@@ -80,6 +80,12 @@ _SIGS = {
     "kmx_kronmult_batched_grad_f32": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp],
     "kmx_kronmult_xbatched_wide": [_i, _i, _i, _vp, _i, _vp, _vp, _i, _optp, _vp],
     "kmx_kronmult_mixed_f64": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
+    "kmx_xbatched_build_f64": [_i, _vp, C.c_longlong, C.c_longlong, _i, _vp, C.c_longlong, _i,
+                               _vp, C.c_longlong, _i, _vp, _vp, _vp, _i, _i, _vp, _sz, _vp, _vp,
+                               _vp, _vp],
+    "kmx_xbatched_build_f32": [_i, _vp, C.c_longlong, C.c_longlong, _i, _vp, C.c_longlong, _i,
+                               _vp, C.c_longlong, _i, _vp, _vp, _vp, _i, _i, _vp, _sz, _vp, _vp,
+                               _vp, _vp],
     "kmx_kgemm_nn_batched_f64": [_i, _i, _i, C.c_double, _vp, _vp, _vp, _vp, C.c_double, _vp, _vp,
                                  _i, _vp],
     "kmx_kgemm_nt_batched_f64": [_i, _i, _i, C.c_double, _vp, _vp, _vp, _vp, C.c_double, _vp, _vp,
@@ -125,6 +131,8 @@ def lib():
             L.kmx_grad_workspace_bytes.argtypes = [_i, _i, _i, _i]
             L.kmx_grad_workspace_bytes.restype = C.c_size_t
             L.kmx_deterministic_workspace_bytes.argtypes = [_i]
+            L.kmx_xbatched_build_workspace_bytes.restype = _sz
+            L.kmx_xbatched_build_workspace_bytes.argtypes = [_i]
             L.kmx_deterministic_workspace_bytes.restype = C.c_size_t
             L.kmx_version.argtypes = []
             L.kmx_version.restype = C.c_char_p

@@ -208,10 +208,18 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   cudaError_t e;
   const bool sq = is_square(p);
   if (wide_in) {
-    e = wide_in == KMX_IN_BF16 ? launch_wide_bf16(p, h, s) : launch_wide_f32(p, h, s);
+    e = cudaErrorNotSupported;
+    if (o.form == KMX_FORM_TF32X3 && !det)
+      e = wide_in == KMX_IN_BF16 ? launch_tc_wide_bf16(p, s) : launch_tc_wide_f32(p, s);
+    if (e == cudaErrorNotSupported)
+      e = wide_in == KMX_IN_BF16 ? launch_wide_bf16(p, h, s) : launch_wide_f32(p, h, s);
   } else if (!is_f64) {
-    if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
-    e = launch_f32_plain(p, h, s);
+    e = cudaErrorNotSupported;
+    if (o.form == KMX_FORM_TF32X3 && !det) e = launch_tc_f32(p, s);
+    if (e == cudaErrorNotSupported) {
+      if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
+      e = launch_f32_plain(p, h, s);
+    }
   } else {
     int form = o.form;
     if (form == KMX_FORM_AUTO) {

@@ -10,4 +10,8 @@ cudaError_t launch_f64_split(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_f32(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_bf16(Problem& p, const LaunchHint& h, cudaStream_t s);
+// Tensor-core (3xTF32) forms; cudaErrorNotSupported for shapes without a kernel.
+cudaError_t launch_tc_f32(Problem& p, cudaStream_t s);
+cudaError_t launch_tc_wide_f32(Problem& p, cudaStream_t s);
+cudaError_t launch_tc_wide_bf16(Problem& p, cudaStream_t s);
 }  // namespace kmx

@@ -122,3 +122,26 @@ def test_kgemm_argument_checks_without_gpu(kmx):
         assert fn(4, 4, 4, 1.0, 8, 8, 8, 0, 0.0, 8, 8, 2, None) == 2   # no ldB array
         assert fn(4, 4, 4, 1.0, 0, 0, 0, 0, 0.0, 0, 0, 0, None) == 0   # empty batch
         assert fn(0, 4, 4, 1.0, 0, 0, 0, 0, 0.0, 0, 0, 3, None) == 0   # empty matrices
+
+
+def test_xbatched_build_argument_checks_without_gpu(kmx):
+    L = kmx.lib()
+    for fn in (L.kmx_xbatched_build_f64, L.kmx_xbatched_build_f32):
+        ok = [3, 8, 16, 4, 8, 8, 64, 8, 8, 64, 8, 8, 8, 8, 10, 0, 0, 0, 8, 8, 8, None]
+        bad_d = list(ok)
+        bad_d[0] = 7
+        assert fn(*bad_d) == 1
+        neg_stride = list(ok)
+        neg_stride[2] = -1
+        assert fn(*neg_stride) == 1
+        null_idx = list(ok)
+        null_idx[12] = 0
+        assert fn(*null_idx) == 2
+        sort_no_ws = list(ok)
+        sort_no_ws[15] = 1
+        assert fn(*sort_no_ws) == 3
+        empty = list(ok)
+        empty[14] = 0
+        empty[1] = 0
+        assert fn(*empty) == 0
+    assert L.kmx_xbatched_build_workspace_bytes(1000) >= 4 * 4 * 1000
