@@ -51,6 +51,12 @@ typedef enum kmx_form {
   KMX_FORM_PLAIN = 1,  /* native FP64 fused multiply-add */
   KMX_FORM_SPLIT = 2,  /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
                           ~2^-47 relative per operation, FP64 in and out */
+  KMX_FORM_DIGITS = 4, /* FP64 data on the FP16 tensor cores: X and factors as 7 base-2^9
+                          digits with one exponent per entry, exact digit products
+                          (mma.sync), exact FP32 level sums, FP64 out.  Square n = 4
+                          (d = 4, 6) and n = 16 (d = 2, 3), atomic mode; entries whose
+                          result falls far below the entry's scale, or with Inf/NaN, are
+                          recomputed in double-float.  Other shapes: SPLIT. */
   KMX_FORM_TF32X3 = 3  /* FP32-stored data only: tensor cores (mma.sync TF32), each
                           operand split into two TF32 parts, three products, FP32
                           accumulation (~2^-21 relative per product).  Square n = 4

@@ -27,7 +27,7 @@ STATUS = {
     7: "KMX_ERR_OVERLAP",
 }
 
-FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3}
+FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3, "digits": 4}
 ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2}
 ACCUMULATE = {"atomic": 0, "deterministic": 1}
 

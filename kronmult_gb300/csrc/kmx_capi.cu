@@ -35,8 +35,8 @@ std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
 
 // Library-owned workspaces, stream ordered, one per device and purpose
-// (0: deterministic segments, 1: mixed-shape grouping).
-constexpr int WS_SLOTS = 2;
+// (0: deterministic segments, 1: mixed-shape grouping, 2: digits-form redo list).
+constexpr int WS_SLOTS = 3;
 void* g_ws_ptr[WS_SLOTS][MAX_DEVICES];
 size_t g_ws_bytes[WS_SLOTS][MAX_DEVICES];
 bool g_default_init = false;
@@ -226,8 +226,23 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
       const int t = sq ? tuned_form(p.d, p.n[0]) : 0;
       form = t ? t : ((sq && spec_n) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
     }
-    if (h.engine == 0 && sq) h.engine = tuned_engine(form == KMX_FORM_SPLIT ? 2 : 1, p.d, p.n[0]);
-    if (form == KMX_FORM_SPLIT) {
+    if (h.engine == 0 && sq)
+      h.engine = tuned_engine((form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1, p.d,
+                              p.n[0]);
+    if (form == KMX_FORM_DIGITS) {
+      e = cudaErrorNotSupported;
+      if (digits_supported(p)) {
+        void* ws = nullptr;
+        rc = cached_workspace(2, ((size_t)p.count + 64) * sizeof(int), s, &ws);
+        if (rc != KMX_OK) return rc;
+        int* redo_count = static_cast<int*>(ws);
+        e = launch_f64_digits(p, h, redo_count + 64, redo_count, s);
+      }
+      if (e == cudaErrorNotSupported) form = KMX_FORM_SPLIT;
+    }
+    if (form == KMX_FORM_DIGITS) {
+      // launched above
+    } else if (form == KMX_FORM_SPLIT) {
       e = launch_f64_split(p, h, s);
       if (e == cudaErrorNotSupported) e = launch_f64_plain(p, h, s);
     } else if (form == KMX_FORM_PLAIN) {

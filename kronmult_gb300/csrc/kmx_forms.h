@@ -10,6 +10,11 @@ cudaError_t launch_f64_split(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_f32(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_bf16(Problem& p, const LaunchHint& h, cudaStream_t s);
+// FP64 digits form on the FP16 tensor cores: redo (p.count ints) and
+// redo_count are device scratch for the entries handed to the double-float pass.
+bool digits_supported(const Problem& p);
+cudaError_t launch_f64_digits(Problem& p, const LaunchHint& h, int* redo, int* redo_count,
+                              cudaStream_t s);
 // Tensor-core (3xTF32) forms; cudaErrorNotSupported for shapes without a kernel.
 cudaError_t launch_tc_f32(Problem& p, cudaStream_t s);
 cudaError_t launch_tc_wide_f32(Problem& p, cudaStream_t s);

@@ -18,7 +18,7 @@ torch = pytest.importorskip("torch")
 F64_TOL = 1e-13
 F32_TOL = 1e-5
 F32_NORM_TOL = 2e-6
-FORMS = ["plain", "split"]
+FORMS = ["plain", "split", "digits"]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -301,8 +301,9 @@ def test_missing_workspace_for_large_entry(kmx):
         kmx.kronmult_batched(d, n, A, X, Y, None, batch)
 
 
-@pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (5, 3), (3, 5)])
-def test_split_form_extreme_magnitudes(kmx, oracle, d, n):
+@pytest.mark.parametrize("form", ["split", "digits"])
+@pytest.mark.parametrize("d,n", [(6, 4), (4, 8), (5, 3), (3, 5), (4, 4), (3, 16)])
+def test_split_form_extreme_magnitudes(kmx, oracle, d, n, form):
     """Factors scaled by 1e-30..1e30 each and X by 1e-60..1e60 (products stay
     inside FP64 but far outside FP32): the split form rescales every entry by
     powers of two, so its FP32 carriers never overflow or flush."""
@@ -315,7 +316,7 @@ def test_split_form_extreme_magnitudes(kmx, oracle, d, n):
     Yref = np.zeros_like(X)
     oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
     Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
-    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form=form)
     assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
     check_status(kmx)
 
