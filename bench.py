@@ -650,7 +650,8 @@ def run_precision(args):
         pA, pX, pY = ptrs(A64, X64, Yref)
         kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, entries, form="plain")
         Yacc = torch.zeros_like(Yref)
-        for name in ("plain", "split", "f32", "bf16", "f32_tf32x3", "bf16_tf32x3"):
+        for name in ("plain", "split", "f32", "bf16", "f32_tf32x3", "bf16_tf32x3",
+                     "f32_tf32x3_det"):
             if name in ("plain", "split"):
                 A, X = A64, X64
             else:
@@ -661,9 +662,10 @@ def run_precision(args):
                 call = lambda: kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, entries, form=name)
             else:
                 ind = name.split("_")[0]
-                fm = "tf32x3" if name.endswith("tf32x3") else None
+                fm = "tf32x3" if "tf32x3" in name else None
+                acc = "deterministic" if name.endswith("_det") else None
                 call = lambda: kmx.kronmult_xbatched_wide(d, n, pA, n, pX, pY, entries,
-                                                          in_dtype=ind, form=fm)
+                                                          in_dtype=ind, form=fm, accumulate=acc)
             ms = _events_time(torch, call, max(3, args.steps // 2), 2)
             Yacc.zero_()
             call()
@@ -678,7 +680,9 @@ def run_precision(args):
                     "f32_speedup_vs_fp64_chosen": round(res["split"]["ms"] / res["f32"]["ms"], 2),
                     "tf32x3_speedup_vs_fp64_chosen": round(
                         res["split"]["ms"] / res["f32_tf32x3"]["ms"], 2),
-                    "tf32x3_speedup_vs_f32_fma": round(res["f32"]["ms"] / res["f32_tf32x3"]["ms"], 2)})
+                    "tf32x3_speedup_vs_f32_fma": round(res["f32"]["ms"] / res["f32_tf32x3"]["ms"], 2),
+                    "tf32x3_det_speedup_vs_fp64_chosen": round(
+                        res["split"]["ms"] / res["f32_tf32x3_det"]["ms"], 2)})
     kmx.check_device_status()
     print(json.dumps({"metric": "kronmult precision forms, xbatched (GFLOP/s and error vs FP64)",
                       "value": out[0]["f32_speedup_vs_fp64_chosen"], "unit": "ratio",

@@ -209,13 +209,13 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   const bool sq = is_square(p);
   if (wide_in) {
     e = cudaErrorNotSupported;
-    if (o.form == KMX_FORM_TF32X3 && !det)
+    if (o.form == KMX_FORM_TF32X3)
       e = wide_in == KMX_IN_BF16 ? launch_tc_wide_bf16(p, s) : launch_tc_wide_f32(p, s);
     if (e == cudaErrorNotSupported)
       e = wide_in == KMX_IN_BF16 ? launch_wide_bf16(p, h, s) : launch_wide_f32(p, h, s);
   } else if (!is_f64) {
     e = cudaErrorNotSupported;
-    if (o.form == KMX_FORM_TF32X3 && !det) e = launch_tc_f32(p, s);
+    if (o.form == KMX_FORM_TF32X3) e = launch_tc_f32(p, s);
     if (e == cudaErrorNotSupported) {
       if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
       e = launch_f32_plain(p, h, s);

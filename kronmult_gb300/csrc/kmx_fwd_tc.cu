@@ -14,10 +14,13 @@ struct TcKernel {
   int smem;
 };
 
-template <typename In, typename Out>
+template <typename In, typename Out, bool SEG>
 TcKernel pick_tc(int n, int d) {
-#define KMX_TC(NN, D) \
-  if (n == NN && d == D) return {(const void*)tc::tc_kernel<NN, D, In, Out>, tc::smem_bytes(NN, D)};
+#define KMX_TC(NN, D)                                                                         \
+  if constexpr (!SEG || tc::seg_supported(NN, D)) {                                          \
+    if (n == NN && d == D)                                                                    \
+      return {(const void*)tc::tc_kernel<NN, D, In, Out, SEG>, tc::smem_bytes(NN, D)};        \
+  }
   KMX_TC(4, 4)
   KMX_TC(4, 6)
   KMX_TC(8, 3)
@@ -31,8 +34,9 @@ TcKernel pick_tc(int n, int d) {
 
 template <typename In, typename Out>
 cudaError_t launch_tc(Problem& p, cudaStream_t s) {
-  if (!is_square(p) || p.seg_entries) return cudaErrorNotSupported;
-  const TcKernel k = pick_tc<In, Out>(p.n[0], p.d);
+  if (!is_square(p)) return cudaErrorNotSupported;
+  const TcKernel k = p.seg_entries ? pick_tc<In, Out, true>(p.n[0], p.d)
+                                   : pick_tc<In, Out, false>(p.n[0], p.d);
   if (!k.func) return cudaErrorNotSupported;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

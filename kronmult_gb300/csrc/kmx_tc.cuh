@@ -49,6 +49,9 @@ __host__ __device__ constexpr bool supported(int NN, int D) {
 }
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
+__host__ __device__ constexpr int tiles_per_warp_h(int NN, int D) {
+  return (ipow(NN, D) / (NN == 4 ? 16 : NN) / 16 + WARPS - 1) / WARPS;
+}
 
 __device__ __forceinline__ int swz(int a) {
   int u = a >> 5;
@@ -95,6 +98,17 @@ __device__ __forceinline__ float factor(const float* sA, int i, int k) {
 }
 
 template <typename Out>
+__device__ __forceinline__ Out widen(float v);
+template <>
+__device__ __forceinline__ float widen<float>(float v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ double widen<double>(float v) {
+  return tile::SplitPolicy::to_f64(v, 0);
+}
+
+template <typename Out>
 __device__ __forceinline__ void add_out(Out* y, float v);
 template <>
 __device__ __forceinline__ void add_out<float>(float* y, float v) {
@@ -105,18 +119,35 @@ __device__ __forceinline__ void add_out<double>(double* y, float v) {
   atomicAdd(y, tile::SplitPolicy::to_f64(v, 0));
 }
 
-// One GEMM step of one entry.
-template <int NN, int D, int PH, typename In, typename Out>
+// Tiles of one step handled by each warp (compile time, so that a segment's
+// running sums can live in registers indexed by it).
+template <int NN, int D>
+__host__ __device__ constexpr int tiles_per_warp() {
+  return (ipow(NN, D) / ks_of(NN) / 16 + WARPS - 1) / WARPS;
+}
+// Running sums per thread in segment mode: the last step's outputs.
+template <int NN, int D>
+__host__ __device__ constexpr int seg_values() {
+  return tiles_per_warp<NN, D>() * (ks_of(NN) / 8) * 4;
+}
+// Segment mode keeps the running sums in registers: shapes with few outputs per thread.
+__host__ __device__ constexpr bool seg_supported(int NN, int D) {
+  return supported(NN, D) &&
+         (tiles_per_warp_h(NN, D) * (ks_of(NN) / 8) * 4) <= 16;
+}
+
+// One GEMM step of one entry.  SEG: the last step adds into racc instead of Y.
+template <int NN, int D, int PH, bool SEG, typename In, typename Out>
 __device__ __forceinline__ void step(const In* __restrict__ xp, Out* yp, float* Z, const float* sA,
-                                     int warp, int g, int t) {
+                                     int warp, int g, int t, Out* racc) {
   constexpr int NG = group_digits(NN);
   constexpr int P = D / NG;
   constexpr int KS = ks_of(NN);
   constexpr int KB = KS / 8;
   constexpr int M = ipow(NN, D) / KS;
   constexpr int TILES = M / 16;
+  constexpr int TPW = tiles_per_warp<NN, D>();
   constexpr int R = ipow(NN, D - (PH + 1) * NG);
-  static_assert(TILES % WARPS == 0 || TILES < WARPS, "tile split");
   // B fragments (k = 8*ks + t + 4*h, i = 8*nt + g), split once per step
   uint32_t bb[KB][KB][2], bs[KB][KB][2];
 #pragma unroll
@@ -131,8 +162,7 @@ __device__ __forceinline__ void step(const In* __restrict__ xp, Out* yp, float* 
     const int L = row / R, r = row - L * R;  // R is a power of two
     return L * KS * R + k * R + r;
   };
-#pragma unroll 2
-  for (int tile = warp; tile < TILES; tile += WARPS) {
+  auto do_tile = [&](int jt, int tile) {
     const int m0 = tile * 16;
     float av[KB][4];
 #pragma unroll
@@ -167,69 +197,160 @@ __device__ __forceinline__ void step(const In* __restrict__ xp, Out* yp, float* 
     for (int nt = 0; nt < KB; ++nt)
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const int a = addr(m0 + g + 8 * (c >> 1), 8 * nt + 2 * t + (c & 1));
         if constexpr (PH == P - 1) {
-          add_out<Out>(yp + a, acc[nt][c]);
+          if constexpr (SEG) {
+            racc[(jt * KB + nt) * 4 + c] += widen<Out>(acc[nt][c]);
+          } else {
+            add_out<Out>(yp + addr(m0 + g + 8 * (c >> 1), 8 * nt + 2 * t + (c & 1)), acc[nt][c]);
+          }
         } else {
-          Z[swz(a)] = acc[nt][c];
+          Z[swz(addr(m0 + g + 8 * (c >> 1), 8 * nt + 2 * t + (c & 1)))] = acc[nt][c];
         }
       }
+  };
+  if constexpr (SEG) {
+    // compile-time tile index: the running sums racc are indexed by it
+#pragma unroll
+    for (int jt = 0; jt < TPW; ++jt)
+      if (warp + jt * WARPS < TILES) do_tile(jt, warp + jt * WARPS);
+  } else {
+#pragma unroll 2
+    for (int tile = warp; tile < TILES; tile += WARPS) do_tile(0, tile);
   }
 }
 
-template <int NN, int D, int PH, typename In, typename Out>
+template <int NN, int D, int PH, bool SEG, typename In, typename Out>
 __device__ __forceinline__ void steps(const In* xp, Out* yp, float* Z, const float* sA, int warp,
-                                      int g, int t) {
+                                      int g, int t, Out* racc) {
   constexpr int P = D / group_digits(NN);
-  step<NN, D, PH, In, Out>(xp, yp, Z, sA, warp, g, t);
+  step<NN, D, PH, SEG, In, Out>(xp, yp, Z, sA, warp, g, t, racc);
   if constexpr (PH + 1 < P) {
     __syncthreads();  // step PH's Z complete
-    steps<NN, D, PH + 1, In, Out>(xp, yp, Z, sA, warp, g, t);
+    steps<NN, D, PH + 1, SEG, In, Out>(xp, yp, Z, sA, warp, g, t, racc);
   }
+}
+
+// Y address of running sum v of this thread (segment mode).
+template <int NN, int D>
+__device__ __forceinline__ int seg_addr(int v, int warp, int g, int t) {
+  constexpr int KS = ks_of(NN);
+  constexpr int KB = KS / 8;
+  const int c = v & 3, nt = (v >> 2) % KB, jt = (v >> 2) / KB;
+  const int row = (warp + jt * WARPS) * 16 + g + 8 * (c >> 1);
+  return row * KS + 8 * nt + 2 * t + (c & 1);  // last step: R = 1
 }
 
 __host__ __device__ constexpr int smem_bytes(int NN, int D) {
-  return (ipow(NN, D) + D * NN * NN) * 4 + 16;
+  return (ipow(NN, D) + D * NN * NN) * 4 + 16;  // Z, factors, flag and segment words
 }
 
-// Persistent: each CTA takes entries in grid-stride order.
-template <int NN, int D, typename In, typename Out>
+// Loads the entry's factors into shared memory; returns (in *s_null) whether
+// any pointer of the entry is NULL.
+template <int NN, int D, typename In>
+__device__ __forceinline__ void load_factors(const Problem& p, long long ent, float* sA,
+                                             int* s_null) {
+  for (int idx = threadIdx.x; idx < D * NN * NN; idx += THREADS) {
+    const int l = idx / (NN * NN), rem = idx - l * NN * NN;
+    const int i = rem / NN, k = rem - i * NN;
+    const In* Ap = tile::a_ptr<In>(p, ent, l);
+    float v = 0.f;
+    if (Ap) {
+      const long long ld = p.ld[l];
+      v = to_f32(p.trans ? Ap[k + i * ld] : Ap[i + k * ld]);
+    } else {
+      *s_null = 1;
+    }
+    sA[idx] = v;  // sA[l][i][k] = A_l(i, k), or A_l(k, i) when transposed
+  }
+}
+
+// Persistent kernel.
+//   SEG == false: entries in grid-stride order, contributions added to Y
+//     with RED.
+//   SEG == true (deterministic mode): the CTA pops Y segments -- the entries
+//     sharing one Y block, in their original order -- from the device work
+//     queue, sums their contributions in registers (every thread owns the
+//     same output elements for every entry) and adds the sum to the Y block
+//     once, with plain loads and stores (the CTA owns the block).
+template <int NN, int D, typename In, typename Out, bool SEG>
 __global__ void __launch_bounds__(THREADS) tc_kernel(const Problem p) {
   static_assert(supported(NN, D), "no tensor-core kernel for this shape");
+  static_assert(!SEG || seg_supported(NN, D), "segment mode: too many outputs per thread");
   constexpr int N = ipow(NN, D);
+  constexpr int NV = SEG ? seg_values<NN, D>() : 1;
   extern __shared__ __align__(16) unsigned char smem[];
   float* Z = reinterpret_cast<float*>(smem);
   float* sA = Z + N;
   int* s_null = reinterpret_cast<int*>(sA + D * NN * NN);
+  int* s_seg = s_null + 1;  // [segment id, offset, count]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, t = lane & 3;
-  const long long total = launch_count(p);
-  for (long long e = blockIdx.x; e < total; e += gridDim.x) {
-    const long long ent = tile::entry_index(p, e);
-    if (threadIdx.x == 0) *s_null = 0;
-    __syncthreads();  // the previous entry is done with Z and sA
-    for (int idx = threadIdx.x; idx < D * NN * NN; idx += THREADS) {
-      const int l = idx / (NN * NN), rem = idx - l * NN * NN;
-      const int i = rem / NN, k = rem - i * NN;
-      const In* Ap = tile::a_ptr<In>(p, ent, l);
-      float v = 0.f;
-      if (Ap) {
-        const long long ld = p.ld[l];
-        v = to_f32(p.trans ? Ap[k + i * ld] : Ap[i + k * ld]);
-      } else {
-        *s_null = 1;
+  if constexpr (!SEG) {
+    const long long total = launch_count(p);
+    for (long long e = blockIdx.x; e < total; e += gridDim.x) {
+      const long long ent = tile::entry_index(p, e);
+      if (threadIdx.x == 0) *s_null = 0;
+      __syncthreads();  // the previous entry is done with Z and sA
+      load_factors<NN, D, In>(p, ent, sA, s_null);
+      const In* xp = tile::x_ptr<In>(p, ent);
+      Out* yp = tile::y_ptr<Out>(p, ent);
+      if (threadIdx.x == 0 && (!xp || !yp)) *s_null = 1;
+      __syncthreads();
+      if (*s_null) {
+        if (threadIdx.x == 0) atomicOr(p.status, DF_NULL_PTR);
+        continue;
       }
-      sA[idx] = v;  // sA[l][i][k] = A_l(i, k), or A_l(k, i) when transposed
+      steps<NN, D, 0, false, In, Out>(xp, yp, Z, sA, warp, g, t, nullptr);
     }
-    const In* xp = tile::x_ptr<In>(p, ent);
-    Out* yp = tile::y_ptr<Out>(p, ent);
-    if (threadIdx.x == 0 && (!xp || !yp)) *s_null = 1;
-    __syncthreads();
-    if (*s_null) {
-      if (threadIdx.x == 0) atomicOr(p.status, DF_NULL_PTR);
-      continue;
+  } else {
+    for (;;) {
+      __syncthreads();  // the previous segment is done with s_seg
+      if (threadIdx.x == 0) {
+        const int q = atomicAdd(p.seg_queue, 1);
+        if (q < *p.seg_num) {
+          const int sid = p.seg_order[q];
+          s_seg[0] = 1;
+          s_seg[1] = p.seg_offset[sid];
+          s_seg[2] = p.seg_count[sid];
+        } else {
+          s_seg[0] = 0;
+        }
+      }
+      __syncthreads();
+      if (!s_seg[0]) break;
+      const int off = s_seg[1], cnt = s_seg[2];
+      Out racc[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) racc[v] = Out(0);
+      Out* yseg = nullptr;
+      for (int j = 0; j < cnt; ++j) {
+        const long long ent = p.seg_entries[off + j];
+        __syncthreads();  // the previous entry is done with Z, sA and s_null
+        if (threadIdx.x == 0) *s_null = 0;
+        __syncthreads();
+        load_factors<NN, D, In>(p, ent, sA, s_null);
+        const In* xp = tile::x_ptr<In>(p, ent);
+        Out* yp = tile::y_ptr<Out>(p, ent);
+        yseg = yp;  // every entry of a segment has the same Y block
+        if (threadIdx.x == 0 && (!xp || !yp)) *s_null = 1;
+        __syncthreads();
+        if (*s_null) {
+          if (threadIdx.x == 0) atomicOr(p.status, DF_NULL_PTR);
+          continue;
+        }
+        steps<NN, D, 0, true, In, Out>(xp, yp, Z, sA, warp, g, t, racc);
+      }
+      if (yseg) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const int jt = (v >> 2) / (ks_of(NN) / 8);
+          if (warp + jt * WARPS < N / ks_of(NN) / 16) {
+            Out* y = yseg + seg_addr<NN, D>(v, warp, g, t);
+            *y += racc[v];
+          }
+        }
+      }
     }
-    steps<NN, D, 0, In, Out>(xp, yp, Z, sA, warp, g, t);
   }
 }
 

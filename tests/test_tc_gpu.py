@@ -127,3 +127,55 @@ def test_tf32x3_null_entry_flagged(kmx):
         kmx.check_device_status()
     y = Y.cpu().numpy()
     assert not y[3].any() and y[0].any() and y[5].any()
+
+
+@pytest.mark.parametrize("d,n", TC_SHAPES)
+@pytest.mark.parametrize("in_dtype", ["f32", "bf16"])
+def test_tf32x3_deterministic_segments(kmx, oracle, d, n, in_dtype):
+    """Deterministic mode: entries grouped by Y block, each block's
+    contributions summed in a fixed order in registers and written once;
+    bitwise identical across calls.  (d=5, n=8 has no segment kernel and runs
+    the FP32-FMA segment kernel.)"""
+    rng = np.random.default_rng(400 + 10 * d + n)
+    A, X, Y0, y_idx, x_idx, a_idx = _case(rng, d, n)
+    pool = A.shape[1]
+    tdt = torch.float32 if in_dtype == "f32" else torch.bfloat16
+    Ad = torch.from_numpy(A).to(tdt).cuda()
+    Xd = torch.from_numpy(X).to(tdt).cuda()
+    Yref = Y0.copy()
+    oracle.xbatched_idx(d, n, Ad.double().cpu().numpy(), n, pool, Xd.double().cpu().numpy(), Yref,
+                        y_idx, x_idx, a_idx)
+    N = n ** d
+    esz = Ad.element_size()
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel(), esz)
+    pX = kmx.pointer_array(Xd, x_idx * N, esz)
+    outs = []
+    for _ in range(2):
+        Yd = torch.from_numpy(Y0.copy()).cuda()
+        kmx.kronmult_xbatched_wide(d, n, pA, n, pX, kmx.pointer_array(Yd, y_idx * N), len(y_idx),
+                                   in_dtype=in_dtype, form="tf32x3", accumulate="deterministic")
+        outs.append(Yd)
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+    assert torch.equal(outs[0], outs[1])
+    err = blockwise_rel_err(outs[0].cpu().numpy() - Y0, Yref - Y0)
+    assert err <= TC_TOL, err
+
+
+def test_tf32x3_deterministic_f32_entry_point(kmx, oracle):
+    d, n = 4, 8
+    rng = np.random.default_rng(9)
+    A, X, Y0, y_idx, x_idx, a_idx = _case(rng, d, n)
+    pool = A.shape[1]
+    A32, X32, Y32 = A.astype(np.float32), X.astype(np.float32), Y0.astype(np.float32)
+    Yref = Y32.astype(np.float64)
+    oracle.xbatched_idx(d, n, A32.astype(np.float64), n, pool, X32.astype(np.float64), Yref,
+                        y_idx, x_idx, a_idx)
+    Ad, Xd, Yd = (torch.from_numpy(v).cuda() for v in (A32, X32, Y32.copy()))
+    pA, pX, pY = _pointers(kmx, Ad, Xd, Yd, y_idx, x_idx, a_idx, d, n, pool)
+    kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, len(y_idx), dtype=torch.float32,
+                          form="tf32x3", accumulate="deterministic")
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+    err = blockwise_rel_err(Yd.cpu().numpy().astype(np.float64) - Y32, Yref - Y32)
+    assert err <= TC_TOL, err
