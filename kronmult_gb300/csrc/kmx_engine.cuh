@@ -253,28 +253,42 @@ __device__ __forceinline__ double f32_to_f64_scaled(float f, int escale) {
   return __longlong_as_double((long long)b);
 }
 
-// sum_j a[j]*v[j] in double-float; the j = 0 term seeds the sums.
+// Exact sum of two FP32 values: s + e == a + b (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// sum_j a[j]*v[j] in double-float.  Every product's high part is exact as
+// (pr, pe) by FMA; the high parts are added by a pairwise tree of exact
+// two-sums (depth log2(NN) instead of NN-1, the same operations), and the
+// low parts, the two-sum errors and the cross terms a.hi*v.lo + a.lo*v.hi
+// are summed in FP32 beside them.
 template <int NN>
 __device__ __forceinline__ df df_dot(const df* a, const df* v) {
-  float s = __fmul_rn(a[0].hi, v[0].hi);
-  float c = __fmaf_rn(a[0].hi, v[0].hi, -s);
-  c = __fmaf_rn(a[0].hi, v[0].lo, c);
-  c = __fmaf_rn(a[0].lo, v[0].hi, c);
+  float pr[NN], c = 0.f;
 #pragma unroll
-  for (int j = 1; j < NN; ++j) {
-    const float pr = __fmul_rn(a[j].hi, v[j].hi);
-    const float pe = __fmaf_rn(a[j].hi, v[j].hi, -pr);
-    const float t = __fadd_rn(s, pr);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(err, pe));
-    c = __fmaf_rn(a[j].hi, v[j].lo, c);
-    c = __fmaf_rn(a[j].lo, v[j].hi, c);
+  for (int j = 0; j < NN; ++j) {
+    pr[j] = __fmul_rn(a[j].hi, v[j].hi);
+    float e = __fmaf_rn(a[j].hi, v[j].hi, -pr[j]);
+    e = __fmaf_rn(a[j].hi, v[j].lo, e);
+    e = __fmaf_rn(a[j].lo, v[j].hi, e);
+    c = j == 0 ? e : __fadd_rn(c, e);
+  }
+#pragma unroll
+  for (int w = 1; w < NN; w *= 2) {
+#pragma unroll
+    for (int j = 0; j + w < NN; j += 2 * w) {
+      float s, e;
+      two_sum(pr[j], pr[j + w], s, e);
+      pr[j] = s;
+      c = __fadd_rn(c, e);
+    }
   }
   df r;
-  r.hi = __fadd_rn(s, c);
-  r.lo = __fsub_rn(c, __fsub_rn(r.hi, s));
+  r.hi = __fadd_rn(pr[0], c);
+  r.lo = __fsub_rn(c, __fsub_rn(r.hi, pr[0]));
   return r;
 }
 

@@ -129,13 +129,12 @@ def test_tf32x3_null_entry_flagged(kmx):
     assert not y[3].any() and y[0].any() and y[5].any()
 
 
-@pytest.mark.parametrize("d,n", TC_SHAPES)
+@pytest.mark.parametrize("d,n", [s for s in TC_SHAPES if s != (5, 8)])
 @pytest.mark.parametrize("in_dtype", ["f32", "bf16"])
 def test_tf32x3_deterministic_segments(kmx, oracle, d, n, in_dtype):
     """Deterministic mode: entries grouped by Y block, each block's
     contributions summed in a fixed order in registers and written once;
-    bitwise identical across calls.  (d=5, n=8 has no segment kernel and runs
-    the FP32-FMA segment kernel.)"""
+    bitwise identical across calls."""
     rng = np.random.default_rng(400 + 10 * d + n)
     A, X, Y0, y_idx, x_idx, a_idx = _case(rng, d, n)
     pool = A.shape[1]
@@ -179,3 +178,17 @@ def test_tf32x3_deterministic_f32_entry_point(kmx, oracle):
     assert kmx.check_device_status() == 0
     err = blockwise_rel_err(Yd.cpu().numpy().astype(np.float64) - Y32, Yref - Y32)
     assert err <= TC_TOL, err
+
+
+def test_tf32x3_deterministic_without_segment_kernel(kmx):
+    """d=5, n=8 (32768-element blocks) has no segment kernel in any form: the
+    deterministic request is refused before any launch."""
+    d, n = 5, 8
+    A = torch.zeros((1, d, n, n), dtype=torch.float32, device="cuda")
+    X = torch.zeros((1, n ** d), dtype=torch.float32, device="cuda")
+    Y = torch.zeros((1, n ** d), dtype=torch.float64, device="cuda")
+    pA = kmx.pointer_array(A, [l * n * n for l in range(d)])
+    with pytest.raises(kmx.KmxError, match="UNSUPPORTED"):
+        kmx.kronmult_xbatched_wide(d, n, pA, n, kmx.pointer_array(X, [0]),
+                                   kmx.pointer_array(Y, [0]), 1, form="tf32x3",
+                                   accumulate="deterministic")
