@@ -190,6 +190,43 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_kernel(KgArgs<T> a) {
   }
 }
 
+// Small matrices (mm*nn <= 2048): one warp per entry, each lane computes
+// outputs in a strided loop straight from global memory (the entry's A and
+// B stay in L1); no shared memory, no block barriers.
+template <typename T, bool TRANS_B>
+__global__ void __launch_bounds__(KG_THREADS) kgemm_small_kernel(KgArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (KG_THREADS / 32);
+  const int outs = a.mm * a.nn;
+  for (long long e = (long long)blockIdx.x * (KG_THREADS / 32) + (threadIdx.x >> 5); e < a.items;
+       e += warps) {
+    const T* __restrict__ Ap = a.A[e];
+    const T* __restrict__ Bp = a.B[e];
+    T* Cp = a.C[e];
+    const long long lda = a.ldA[e], ldb = a.ldB[e], ldc = a.ldC[e];
+    const bool need_ab = a.kk > 0;
+    if (Cp == nullptr || (need_ab && (Ap == nullptr || Bp == nullptr))) {
+      if (lane == 0) atomicOr(a.status, DF_NULL_PTR);
+      continue;
+    }
+    if (ldc < a.mm || (need_ab && (lda < a.mm || ldb < (TRANS_B ? a.nn : a.kk)))) {
+      if (lane == 0) atomicOr(a.status, DF_BAD_SHAPE);
+      continue;
+    }
+    for (int o = lane; o < outs; o += 32) {
+      const int j = o / a.mm, i = o - j * a.mm;
+      Acc<T> acc;
+      acc.zero();
+      for (int k = 0; k < a.kk; ++k) {
+        const T av = __ldg(Ap + i + k * lda);
+        const T bv = TRANS_B ? __ldg(Bp + j + k * ldb) : __ldg(Bp + k + j * ldb);
+        acc.add(av, bv);
+      }
+      acc.template store<TRANS_B>(Cp + i + j * ldc, a.alpha, a.beta);
+    }
+  }
+}
+
 struct KgConfig {
   const void* func;
   int bm, bn;
@@ -212,7 +249,14 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   if (batch == 0 || mm == 0 || nn == 0) return KMX_OK;
   if (!C || !ldC) return KMX_ERR_NULL_POINTER;
   if (kk > 0 && (!A || !ldA || !B || !ldB)) return KMX_ERR_NULL_POINTER;
-  const KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
+  const bool small = (long long)mm * nn <= 2048;
+  KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
+  if (small) {
+    cfg.func = trans_b ? (const void*)kgemm_small_kernel<T, true>
+                       : (const void*)kgemm_small_kernel<T, false>;
+    cfg.bm = mm;
+    cfg.bn = nn;
+  }
   KgArgs<T> ka;
   ka.mm = mm;
   ka.nn = nn;
@@ -227,7 +271,7 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   ka.ldC = ldC;
   ka.tiles_m = (mm + cfg.bm - 1) / cfg.bm;
   ka.tiles_n = (nn + cfg.bn - 1) / cfg.bn;
-  ka.items = (long long)batch * ka.tiles_m * ka.tiles_n;
+  ka.items = (long long)batch * ka.tiles_m * ka.tiles_n;  // small kernel: one item per entry
   int rc = device_status_ptr(&ka.status);
   if (rc != KMX_OK) return rc;
   int dev = 0;
@@ -237,7 +281,8 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.func, KG_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   long long grid = (long long)di.sms * per_sm;
-  if (grid > ka.items) grid = ka.items;
+  const long long cta_items = small ? (ka.items + KG_THREADS / 32 - 1) / (KG_THREADS / 32) : ka.items;
+  if (grid > cta_items) grid = cta_items;
   void* args[] = {&ka};
   const cudaError_t e = cudaLaunchKernel(cfg.func, dim3((unsigned)grid), dim3(KG_THREADS), args, 0, s);
   return e == cudaSuccess ? KMX_OK : KMX_ERR_CUDA;

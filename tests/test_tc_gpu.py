@@ -129,12 +129,12 @@ def test_tf32x3_null_entry_flagged(kmx):
     assert not y[3].any() and y[0].any() and y[5].any()
 
 
-@pytest.mark.parametrize("d,n", [s for s in TC_SHAPES if s != (5, 8)])
+@pytest.mark.parametrize("d,n", [s for s in TC_SHAPES if s != (5, 8) and s[0] >= 3])
 @pytest.mark.parametrize("in_dtype", ["f32", "bf16"])
 def test_tf32x3_deterministic_segments(kmx, oracle, d, n, in_dtype):
     """Deterministic mode: entries grouped by Y block, each block's
     contributions summed in a fixed order in registers and written once;
-    bitwise identical across calls."""
+    bitwise identical across calls.  (The deterministic mode takes d >= 3.)"""
     rng = np.random.default_rng(400 + 10 * d + n)
     A, X, Y0, y_idx, x_idx, a_idx = _case(rng, d, n)
     pool = A.shape[1]
