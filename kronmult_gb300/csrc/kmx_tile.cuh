@@ -418,6 +418,17 @@ __host__ __device__ constexpr int group_smem_bytes() {
   return off_acc<Pol, NN, D>() + (SEG ? acc_bytes<Pol, NN, D>() : 0);
 }
 
+// The plain-FP64 evaluation of an entry with Inf/NaN, kept out of line: it
+// is rarely taken, and inlined it would sit in the hot loop's instruction
+// stream.
+template <int NN>
+__device__ __noinline__ void nonfinite_entry(const Problem& p, long long ent, double* sA,
+                                             double* buf, int lt, int G, int g) {
+  EntryPtrs<double> en;
+  resolve_entry<double>(p, ent, en);
+  sq_plain_entry<double, NN, false>(p, en, sA, buf, lt, G, g);
+}
+
 enum : int { TF_NULL = 1, TF_TIMEOUT = 2 };
 enum : int { ED_VALID = 1, ED_FIRST = 2 };  // entry descriptor flags
 
@@ -710,10 +721,8 @@ tile_kernel(const Problem p) {
           // Inf/NaN propagate exactly as in FP64: plain FP64 on the same
           // shared memory (an all-zero factor or X contributes exactly zero).
           if (nonfinite) {
-            EntryPtrs<double> en;
-            resolve_entry<double>(p, ent, en);
-            sq_plain_entry<double, NN, false>(p, en, reinterpret_cast<double*>(sA),
-                                              reinterpret_cast<double*>(buf), lt, G, g);
+            nonfinite_entry<NN>(p, ent, reinterpret_cast<double*>(sA),
+                                reinterpret_cast<double*>(buf), lt, G, g);
             group_sync(g, G);
           }
         }
