@@ -273,7 +273,7 @@ __device__ __forceinline__ void load_factors(const Problem& p, long long ent, fl
 //     same output elements for every entry) and adds the sum to the Y block
 //     once, with plain loads and stores (the CTA owns the block).
 template <int NN, int D, typename In, typename Out, bool SEG>
-__global__ void __launch_bounds__(THREADS, SEG ? 2 : 1) tc_kernel(const Problem p) {
+__global__ void __launch_bounds__(THREADS, SEG ? 2 : 4) tc_kernel(const Problem p) {
   static_assert(supported(NN, D), "no tensor-core kernel for this shape");
   static_assert(!SEG || seg_supported(NN, D), "segment mode: too many outputs per thread");
   constexpr int N = ipow(NN, D);
