@@ -97,14 +97,20 @@ __device__ __forceinline__ void mode_gram(const T* B, const T* Fk, T* sdA, T* sR
 #pragma unroll
         for (int b = 0; b < NN; ++b) acc[a * NN + b] = fma(bv[a], x[b], acc[a * NN + b]);
     }
+    // neighbouring lanes pre-add their partials (one shuffle and one add per
+    // partial), halving the shared-memory partials
+    const int GH = G / 2;
 #pragma unroll
-    for (int q = 0; q < NN2; ++q) sRed[q * G + lt] = acc[q];
+    for (int q = 0; q < NN2; ++q) {
+      const T other = __shfl_down_sync(0xffffffffu, acc[q], 1);
+      if ((lt & 1) == 0) sRed[q * GH + (lt >> 1)] = acc[q] + other;
+    }
     __syncthreads();
-    const int nch = G / 32;
-    T* sRed2 = sRed + NN2 * G;
+    const int nch = GH / 32;
+    T* sRed2 = sRed + NN2 * GH;
     for (int t = lt; t < NN2 * nch; t += G) {
       const int q = t / nch, c = t - q * nch;
-      const T* src = sRed + q * G + c * 32;
+      const T* src = sRed + q * GH + c * 32;
       T v = src[0];
 #pragma unroll 8
       for (int i = 1; i < 32; ++i) v += src[i];
@@ -134,7 +140,7 @@ __device__ __forceinline__ void mode_gram(const T* B, const T* Fk, T* sdA, T* sR
 
 // sA holds A_l row-major: sA[l*NN*NN + a*NN + j] = A_l(a, j).
 template <typename T, int NN>
-__global__ void __launch_bounds__(256) grad_kernel(const GradProblem gp) {
+__global__ void __launch_bounds__(NN <= 5 ? 512 : 256) grad_kernel(const GradProblem gp) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NN2 = NN * NN;
   const int d = gp.d, N = gp.N, F = N / NN;
@@ -143,7 +149,7 @@ __global__ void __launch_bounds__(256) grad_kernel(const GradProblem gp) {
   T* sdA = sA + MAXD * NN2;
   T* sB = sdA + MAXD * NN2;
   T* sRed = sB + N;                                            // Gram partial sums (NN <= 5)
-  T* sF = sRed + (NN <= 5 ? NN2 * (G + G / 32) : 0);           // forward intermediates, if they fit
+  T* sF = sRed + (NN <= 5 ? NN2 * (G / 2 + G / 64) : 0);      // forward intermediates, if they fit
   const long long slot = blockIdx.x;
   T* Fst = gp.f_in_smem ? sF
                         : (gp.W ? static_cast<T*>(gp.W) + slot * gp.wslot : nullptr);
@@ -253,28 +259,36 @@ struct GradPlan {
   bool ok;
 };
 
+// Threads: one fiber per thread up to 512 for n <= 5 and 256 above (the
+// fused kernel is FP64-pipe bound and needs many warps to hide the FP64 and
+// shared-memory latency; large entries hold one CTA per SM in shared memory;
+// n > 5 keeps 256 so that its kernels are not capped at 128 registers),
+// multiples of 64 (the Gram reduction pairs lanes).  Falls back to fewer
+// threads when the Gram scratch does not fit.
 template <typename T>
 GradPlan grad_plan(int d, int n, long long N, int max_smem) {
   GradPlan g;
-  int threads = (int)((N / n + 31) / 32 * 32);
+  int threads = (int)((N / n + 63) / 64 * 64);
   if (threads < 64) threads = 64;
-  if (threads > 256) threads = 256;
-  g.threads = threads;
-  const size_t red = n <= 5 ? (size_t)n * n * (threads + threads / 32) * sizeof(T) : 0;
-  const size_t head = 2 * (size_t)MAXD * n * n * sizeof(T) + red;
-  const size_t with_f = head + (size_t)N * sizeof(T) * (d > 1 ? d : 1);
-  const size_t without_f = head + (size_t)N * sizeof(T);
-  g.slot_bytes = (size_t)(d > 1 ? d - 1 : 1) * N * sizeof(T);
-  if (with_f <= 200 * 1024) {
-    g.f_in_smem = 1;
-    g.smem = with_f;
-    g.ok = true;
-  } else {
-    g.f_in_smem = 0;
-    g.smem = without_f;
-    g.ok = without_f <= (size_t)max_smem;
+  if (threads > (n <= 5 ? 512 : 256)) threads = n <= 5 ? 512 : 256;  // the kernels' launch bounds
+  for (;; threads /= 2) {
+    g.threads = threads;
+    const size_t red = n <= 5 ? (size_t)n * n * (threads / 2 + threads / 64) * sizeof(T) : 0;
+    const size_t head = 2 * (size_t)MAXD * n * n * sizeof(T) + red;
+    const size_t with_f = head + (size_t)N * sizeof(T) * (d > 1 ? d : 1);
+    const size_t without_f = head + (size_t)N * sizeof(T);
+    g.slot_bytes = (size_t)(d > 1 ? d - 1 : 1) * N * sizeof(T);
+    if (with_f <= 200 * 1024) {
+      g.f_in_smem = 1;
+      g.smem = with_f;
+      g.ok = true;
+    } else {
+      g.f_in_smem = 0;
+      g.smem = without_f;
+      g.ok = without_f <= (size_t)max_smem;
+    }
+    if (g.ok || threads <= 64) return g;
   }
-  return g;
 }
 
 template <typename T>
