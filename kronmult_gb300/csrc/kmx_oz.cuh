@@ -77,7 +77,6 @@ struct Smem {
   __half z[NPLANE][N];         // digit planes of the intermediate, natural index order
   __half f[P][NP][16][16];     // digit planes of each step's factor, [i][k]
   double a[D][NN][NN];         // the entry's factors, [l][i][k] (transposed if asked)
-  int ea[D];                   // per-factor exponent (|A_l| < 2^ea)
   int ef[P];                   // per-step factor exponent (|F| < 2^(ef-1))
   int emax;                    // X block: largest biased exponent
   int flags;                   // OZ_* bits of the entry
@@ -322,7 +321,6 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
   for (long long e = blockIdx.x; e < total; e += gridDim.x) {
     const long long ent = tile::entry_index(p, e);
     __syncthreads();  // the previous entry is done with shared memory
-    if (threadIdx.x < D) S.ea[threadIdx.x] = 0;
     if (threadIdx.x < SH::P) {
       S.ef[threadIdx.x] = 0;
       S.top[threadIdx.x] = 0;
@@ -341,9 +339,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
       if (Ap) {
         const long long ld = p.ld[l];
         v = p.trans ? Ap[k + i * ld] : Ap[i + k * ld];
-        const int ex = exp_field(v);
-        if (ex == 2047) atomicOr(&S.flags, OZ_REDO);
-        atomicMax(&S.ea[l], ex);
+        if (exp_field(v) == 2047) atomicOr(&S.flags, OZ_REDO);
       } else {
         atomicOr(&S.flags, OZ_NULL);
       }
