@@ -227,6 +227,68 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_small_kernel(KgArgs<T> a) {
   }
 }
 
+// Streaming kernels for the kronmult shapes, whose inner dimensions are tiny
+// (kk <= 16) and one output dimension is long:
+//   nn (short-wide, mm <= 16): thread = one column j of C; it reads B(:, j)
+//     (kk contiguous values), keeps A (mm x kk) in shared memory, writes the
+//     mm values of C(:, j) -- a warp sweeps 32 consecutive columns, so B and C
+//     stream through in full sectors;
+//   nt (tall-narrow, nn <= 16): thread = one row i of C; it reads A(i, :)
+//     (kk values, stride ldA), keeps B (nn x kk) in shared memory, writes the
+//     nn values of C(i, :) -- consecutive threads take consecutive rows.
+// Items are (entry, chunk of 256 columns / rows), grid-stride.
+constexpr int KG_SMALL_DIM = 16;
+template <typename T, bool TRANS_B>
+__global__ void __launch_bounds__(KG_THREADS) kgemm_stream_kernel(KgArgs<T> a) {
+  __shared__ T S[KG_SMALL_DIM * KG_SMALL_DIM];  // A (nn form) or B (nt form), column-major
+  const int tid = threadIdx.x;
+  const int big = TRANS_B ? a.mm : a.nn;         // the long dimension
+  const int chunks = (big + KG_THREADS - 1) / KG_THREADS;
+  for (long long item = blockIdx.x; item < a.items; item += gridDim.x) {
+    const int e = (int)(item / chunks);
+    const int c0 = (int)(item - (long long)e * chunks) * KG_THREADS;
+    const T* __restrict__ Ap = a.A[e];
+    const T* __restrict__ Bp = a.B[e];
+    T* Cp = a.C[e];
+    const long long lda = a.ldA[e], ldb = a.ldB[e], ldc = a.ldC[e];
+    const bool need_ab = a.kk > 0;
+    __syncthreads();  // the previous item is done with S
+    if (Cp == nullptr || (need_ab && (Ap == nullptr || Bp == nullptr))) {
+      if (tid == 0 && c0 == 0) atomicOr(a.status, DF_NULL_PTR);
+      continue;
+    }
+    if (ldc < a.mm || (need_ab && (lda < a.mm || ldb < (TRANS_B ? a.nn : a.kk)))) {
+      if (tid == 0 && c0 == 0) atomicOr(a.status, DF_BAD_SHAPE);
+      continue;
+    }
+    // the small operand: A (mm x kk) for nn, B (nn x kk) for nt, as S[r + k*16]
+    const int rows = TRANS_B ? a.nn : a.mm;
+    for (int idx = tid; idx < rows * a.kk; idx += KG_THREADS) {
+      const int r = idx % rows, k = idx / rows;
+      S[r + k * KG_SMALL_DIM] = TRANS_B ? Bp[r + k * ldb] : Ap[r + k * lda];
+    }
+    __syncthreads();
+    const int c = c0 + tid;
+    if (c >= big) continue;
+    T v[KG_SMALL_DIM];
+#pragma unroll
+    for (int k = 0; k < KG_SMALL_DIM; ++k)
+      if (k < a.kk) v[k] = TRANS_B ? __ldg(Ap + c + k * lda) : __ldg(Bp + k + (long long)c * ldb);
+#pragma unroll
+    for (int r = 0; r < KG_SMALL_DIM; ++r) {
+      if (r >= rows) break;
+      Acc<T> acc;
+      acc.zero();
+#pragma unroll
+      for (int k = 0; k < KG_SMALL_DIM; ++k)
+        if (k < a.kk) acc.add(S[r + k * KG_SMALL_DIM], v[k]);
+      // nn: C(r, c); nt: C(c, r)
+      T* p = TRANS_B ? Cp + c + r * ldc : Cp + r + (long long)c * ldc;
+      acc.template store<TRANS_B>(p, a.alpha, a.beta);
+    }
+  }
+}
+
 struct KgConfig {
   const void* func;
   int bm, bn;
@@ -250,8 +312,17 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   if (!C || !ldC) return KMX_ERR_NULL_POINTER;
   if (kk > 0 && (!A || !ldA || !B || !ldB)) return KMX_ERR_NULL_POINTER;
   const bool small = (long long)mm * nn <= 2048;
+  // streaming: tiny inner and short dimension, long other dimension
+  const bool stream = !small && kk <= KG_SMALL_DIM &&
+                      (trans_b ? (nn <= KG_SMALL_DIM) : (mm <= KG_SMALL_DIM));
   KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
-  if (small) {
+  if (stream) {
+    cfg.func = trans_b ? (const void*)kgemm_stream_kernel<T, true>
+                       : (const void*)kgemm_stream_kernel<T, false>;
+    // items: (entry, chunk of KG_THREADS along the long dimension)
+    cfg.bm = trans_b ? KG_THREADS : mm;
+    cfg.bn = trans_b ? nn : KG_THREADS;
+  } else if (small) {
     cfg.func = trans_b ? (const void*)kgemm_small_kernel<T, true>
                        : (const void*)kgemm_small_kernel<T, false>;
     cfg.bm = mm;
