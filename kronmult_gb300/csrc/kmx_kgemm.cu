@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_small_kernel(KgArgs<T> a) {
   }
 }
 
-// Streaming kernels for the kronmult shapes, whose inner dimensions are tiny
-// (kk <= 16) and one output dimension is long:
+// Streaming kernels (FP32) for the kronmult shapes, whose inner dimensions
+// are tiny (kk <= 16) and one output dimension is long:
 //   nn (short-wide, mm <= 16): thread = one column j of C; it reads B(:, j)
 //     (kk contiguous values), keeps A (mm x kk) in shared memory, writes the
 //     mm values of C(:, j) -- a warp sweeps 32 consecutive columns, so B and C
@@ -312,8 +312,10 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   if (!C || !ldC) return KMX_ERR_NULL_POINTER;
   if (kk > 0 && (!A || !ldA || !B || !ldB)) return KMX_ERR_NULL_POINTER;
   const bool small = (long long)mm * nn <= 2048;
-  // streaming: tiny inner and short dimension, long other dimension
-  const bool stream = !small && kk <= KG_SMALL_DIM &&
+  // streaming: tiny inner and short dimension, long other dimension; FP32
+  // only (these shapes are HBM-bound in FP32, FP64-FMA-bound in FP64, where
+  // the register tiles' several outputs per thread measure faster)
+  const bool stream = sizeof(T) == 4 && !small && kk <= KG_SMALL_DIM &&
                       (trans_b ? (nn <= KG_SMALL_DIM) : (mm <= KG_SMALL_DIM));
   KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
   if (stream) {
