@@ -279,6 +279,8 @@ def run_ours(args):
             step(form, acc=acc)
         e1.record(stream)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         ms = e0.elapsed_time(e1) / K
         if dist:
             t = torch.tensor([ms], device=dev)
