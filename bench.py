@@ -747,6 +747,46 @@ def run_kgemm(args):
                       "hbm_gbs": hbm / 1e9, "cases": out, "data": "synthetic"}))
 
 
+def run_big(args):
+    """Entries beyond one SM: batched FP64 d=6 n=8 (2 MB blocks, 256 entries)
+    and d=5 n=8 (256 KB blocks, 2048 entries), N(0,1)/sqrt(n) factors, N(0,1) X:
+    the split form's two-pass path against the per-mode path with a global
+    intermediate, and plain FP64."""
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    out = []
+    for d, batch in ((6, 256), (5, 2048)):
+        n = 8
+        N = n ** d
+        g = torch.Generator(device="cuda").manual_seed(SEED + d)
+        A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
+        X = torch.randn((batch, N), dtype=torch.float64, device="cuda", generator=g)
+        Y = torch.zeros_like(X)
+        W = torch.zeros_like(X)
+        fl = batch * 2.0 * d * n ** (d + 1)
+        res = {}
+        for name, kw in (("two_pass", dict(form="split")), ("per_mode", dict(form="split", engine="per_mode")),
+                         ("plain", dict(form="plain"))):
+            call = lambda: kmx.kronmult_batched(d, n, A, X, Y, W, batch, **kw)
+            ms = _events_time(torch, call, max(3, args.steps // 2), 2)
+            res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3)}
+        Yr = torch.zeros_like(X)
+        kmx.kronmult_batched(d, n, A, X, Yr, W, batch, form="plain")
+        Y.zero_()
+        kmx.kronmult_batched(d, n, A, X, Y, W, batch, form="split")
+        torch.cuda.synchronize()
+        err = float((torch.linalg.vector_norm(Y - Yr, dim=1) /
+                     torch.linalg.vector_norm(Yr, dim=1)).max())
+        out.append({"d": d, "n": n, "batch": batch, "forms": res, "rel_err_two_pass_vs_plain": err})
+        del A, X, Y, W, Yr
+    kmx.check_device_status()
+    print(json.dumps({"metric": "kronmult GFLOP/s, entries beyond one SM (FP64)",
+                      "value": out[0]["forms"]["two_pass"]["gflops"], "unit": "GFLOP/s",
+                      "workload": "big", "cases": out, "data": "synthetic"}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -756,7 +796,7 @@ def main():
     ap.add_argument("--entries", type=int, default=ENTRIES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["xbatched", "mixed", "grad", "precision", "kgemm"],
+    ap.add_argument("--workload", choices=["xbatched", "mixed", "grad", "precision", "kgemm", "big"],
                     default="xbatched")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -769,6 +809,8 @@ def main():
         return run_precision(args)
     if args.workload == "kgemm":
         return run_kgemm(args)
+    if args.workload == "big":
+        return run_big(args)
     return run_ours(args)
 
 

@@ -292,13 +292,60 @@ def test_null_entry_pointer_sets_device_status(kmx):
 
 
 def test_missing_workspace_for_large_entry(kmx):
-    d, n, batch = 6, 8, 1
+    """Entries beyond shared memory need the caller's W in the per-mode path
+    (the reference's contract); the plain form keeps that path."""
+    d, n, batch = 6, 7, 1
     N = n ** d
     A = torch.rand((batch, d, n, n), dtype=torch.float64, device="cuda")
     X = torch.rand((batch, N), dtype=torch.float64, device="cuda")
     Y = torch.zeros_like(X)
     with pytest.raises(kmx.KmxError, match="WORKSPACE"):
-        kmx.kronmult_batched(d, n, A, X, Y, None, batch)
+        kmx.kronmult_batched(d, n, A, X, Y, None, batch, form="plain")
+
+
+@pytest.mark.parametrize("d", [5, 6])
+@pytest.mark.parametrize("layout", ["batched", "xbatched"])
+def test_two_pass_large_entries_vs_oracle(kmx, oracle, d, layout):
+    """n = 8, d = 5 and 6 (256 KB and 2 MB FP64 blocks) in the split form: two
+    tiled passes through a column-blocked scratch (no caller workspace),
+    against the oracle, including overlapping Y blocks, padded lda and the
+    transposed factors."""
+    n = 8
+    N = n ** d
+    rng = np.random.default_rng(70 + d)
+    if layout == "batched":
+        batch = 3
+        A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+        X = rng.standard_normal((batch, N))
+        Y0 = rng.standard_normal((batch, N))
+        Yref = Y0.copy()
+        oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+        Yd = dev(Y0)
+        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split")
+        assert blockwise_rel_err(host(Yd) - Y0, Yref - Y0) <= F64_TOL
+        At = np.ascontiguousarray(np.swapaxes(A, 2, 3))
+        Yref = np.zeros_like(X)
+        oracle.batched(d, n, At, X.copy(), Yref, np.zeros_like(X), batch)
+        Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", transpose=True)
+        assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    else:
+        pool, nx, ny, ne, lda = 6, 3, 2, 5, n + 3
+        Apool = np.zeros((d, pool, n, lda))
+        Apool[..., :n] = rng.standard_normal((d, pool, n, n)) / np.sqrt(n)
+        Xpool = rng.standard_normal((nx, N))
+        Y0 = rng.standard_normal((ny, N))
+        y_idx = np.array([0, 1, 0, 0, 1])  # overlapping Y blocks
+        x_idx = rng.integers(0, nx, ne)
+        a_idx = rng.integers(0, pool, (ne, d))
+        Yref = Y0.copy()
+        oracle.xbatched_idx(d, n, Apool, lda, pool, Xpool, Yref, y_idx, x_idx, a_idx)
+        Ad, Xd, Yd = dev(Apool), dev(Xpool), dev(Y0)
+        pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * lda).ravel())
+        kmx.kronmult_xbatched(d, n, pA, lda, kmx.pointer_array(Xd, x_idx * N),
+                              kmx.pointer_array(Yd, y_idx * N), None, ne, form="split")
+        assert blockwise_rel_err(host(Yd) - Y0, Yref - Y0) <= F64_TOL
+    check_status(kmx)
 
 
 @pytest.mark.parametrize("form", ["split", "digits"])
