@@ -35,9 +35,8 @@ std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
 
 // Library-owned workspaces, stream ordered, one per device and purpose
-// (0: deterministic segments, 1: mixed-shape grouping, 2: digits-form redo list,
-// 3: two-pass scratch for entries beyond one SM).
-constexpr int WS_SLOTS = 4;
+// (0: deterministic segments, 1: mixed-shape grouping, 2: digits-form redo list).
+constexpr int WS_SLOTS = 3;
 void* g_ws_ptr[WS_SLOTS][MAX_DEVICES];
 size_t g_ws_bytes[WS_SLOTS][MAX_DEVICES];
 bool g_default_init = false;
@@ -243,16 +242,6 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     }
     if (form == KMX_FORM_DIGITS) {
       // launched above
-    } else if (form == KMX_FORM_SPLIT && o.engine == 0 && big_supported(p)) {
-      // entries beyond one SM: two tiled passes instead of d per-mode passes
-      const size_t need = big_workspace_bytes(p.d, p.count);
-      void* ws = nullptr;
-      rc = cached_workspace(3, need, s, &ws);
-      if (rc != KMX_OK) return rc;
-      LaunchHint h1 = h, h2 = h;
-      h1.engine = tuned_engine(2, 3, 8);
-      h2.engine = tuned_engine(2, p.d - 2, 8);
-      e = launch_big_split(p, h2, h1, ws, need, s);
     } else if (form == KMX_FORM_SPLIT) {
       e = launch_f64_split(p, h, s);
       if (e == cudaErrorNotSupported) e = launch_f64_plain(p, h, s);

@@ -65,11 +65,6 @@ struct Problem {
   int trans;             // read every factor transposed
   int y_exclusive;       // Y blocks of distinct entries never overlap
   int* status;           // device status word
-  // Blocked Y layout (tiled kernels, atomic mode): element q of an output
-  // block lives at Y + (q / y_inner) * y_ostride + q % y_inner; y_inner = 0
-  // means contiguous.  Used by the two-pass path for entries beyond one SM.
-  int y_inner;
-  long long y_ostride;
   // execution shape
   int group_threads;     // G
   int groups_per_cta;    // E
@@ -427,10 +422,7 @@ __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs
       T acc = Ad[r * NN] * v[0];
 #pragma unroll
       for (int j = 1; j < NN; ++j) acc = fma(Ad[r * NN + j], v[j], acc);
-      // blocked Y layout (two-pass path for entries beyond one SM), else contiguous
-      const long long yo =
-          p.y_inner ? (long long)(i / p.y_inner) * p.y_ostride + i % p.y_inner : (long long)i;
-      y_accumulate(en.Y + yo, acc, excl);
+      y_accumulate(en.Y + i, acc, excl);
     }
   }
 }

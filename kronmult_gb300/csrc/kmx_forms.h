@@ -15,12 +15,6 @@ cudaError_t launch_wide_bf16(Problem& p, const LaunchHint& h, cudaStream_t s);
 bool digits_supported(const Problem& p);
 cudaError_t launch_f64_digits(Problem& p, const LaunchHint& h, int* redo, int* redo_count,
                               cudaStream_t s);
-// Entries beyond one SM (square n = 8, d = 5, 6), split form: two tiled passes
-// through a column-blocked scratch (ws of big_workspace_bytes(d, count)).
-bool big_supported(const Problem& p);
-size_t big_workspace_bytes(int d, int count);
-cudaError_t launch_big_split(Problem& p, const LaunchHint& h2, const LaunchHint& h1, void* ws,
-                             size_t ws_bytes, cudaStream_t s);
 // Tensor-core (3xTF32) forms; cudaErrorNotSupported for shapes without a kernel.
 cudaError_t launch_tc_f32(Problem& p, cudaStream_t s);
 cudaError_t launch_tc_wide_f32(Problem& p, cudaStream_t s);

@@ -483,7 +483,6 @@ tile_kernel(const Problem p) {
 
   extern __shared__ __align__(16) unsigned char smem[];
   const int E = p.groups_per_cta;
-  const int yin = p.y_inner;  // blocked Y layout (0: contiguous)
   const int g = threadIdx.x / G;
   const int lt = threadIdx.x - g * G;
   if (g >= E) return;
@@ -780,7 +779,7 @@ tile_kernel(const Problem p) {
             acc[q] = a;
           }
         } else {
-          atomicAdd(yp + (yin ? (long long)(q / yin) * p.y_ostride + q % yin : (long long)q), y);
+          atomicAdd(yp + q, y);
         }
       }
     }

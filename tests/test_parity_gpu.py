@@ -305,11 +305,11 @@ def test_missing_workspace_for_large_entry(kmx):
 
 @pytest.mark.parametrize("d", [5, 6])
 @pytest.mark.parametrize("layout", ["batched", "xbatched"])
-def test_two_pass_large_entries_vs_oracle(kmx, oracle, d, layout):
-    """n = 8, d = 5 and 6 (256 KB and 2 MB FP64 blocks) in the split form: two
-    tiled passes through a column-blocked scratch (no caller workspace),
-    against the oracle, including overlapping Y blocks, padded lda and the
-    transposed factors."""
+def test_large_entries_vs_oracle(kmx, oracle, d, layout):
+    """n = 8, d = 5 and 6 (256 KB and 2 MB FP64 blocks, beyond shared memory):
+    the split form on the per-mode kernels with the intermediate in the
+    caller's workspace, against the oracle, including overlapping Y blocks,
+    padded lda and the transposed factors."""
     n = 8
     N = n ** d
     rng = np.random.default_rng(70 + d)
@@ -321,13 +321,14 @@ def test_two_pass_large_entries_vs_oracle(kmx, oracle, d, layout):
         Yref = Y0.copy()
         oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
         Yd = dev(Y0)
-        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split")
+        W = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
+        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, W, batch, form="split")
         assert blockwise_rel_err(host(Yd) - Y0, Yref - Y0) <= F64_TOL
         At = np.ascontiguousarray(np.swapaxes(A, 2, 3))
         Yref = np.zeros_like(X)
         oracle.batched(d, n, At, X.copy(), Yref, np.zeros_like(X), batch)
         Yd = torch.zeros((batch, N), dtype=torch.float64, device="cuda")
-        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", transpose=True)
+        kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, W, batch, form="split", transpose=True)
         assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
     else:
         pool, nx, ny, ne, lda = 6, 3, 2, 5, n + 3
@@ -342,8 +343,11 @@ def test_two_pass_large_entries_vs_oracle(kmx, oracle, d, layout):
         oracle.xbatched_idx(d, n, Apool, lda, pool, Xpool, Yref, y_idx, x_idx, a_idx)
         Ad, Xd, Yd = dev(Apool), dev(Xpool), dev(Y0)
         pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * lda).ravel())
+        Wd = torch.zeros((2 * ne, N), dtype=torch.float64, device="cuda")  # 2 slots per sub-batch
         kmx.kronmult_xbatched(d, n, pA, lda, kmx.pointer_array(Xd, x_idx * N),
-                              kmx.pointer_array(Yd, y_idx * N), None, ne, form="split")
+                              kmx.pointer_array(Yd, y_idx * N),
+                              kmx.pointer_array(Wd, [k * N for k in range(2 * ne)]), ne, ne,
+                              form="split")
         assert blockwise_rel_err(host(Yd) - Y0, Yref - Y0) <= F64_TOL
     check_status(kmx)
 
