@@ -677,6 +677,26 @@ def run_precision(args):
                          torch.linalg.vector_norm(Yref / s, dim=1).clamp_min(1e-300)).max())
             res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
                          "rel_err_vs_fp64_gpu": err}
+        # the FP32 entry point proper: FP32 X, factors and Y (FP32 atomics)
+        A32, X32 = A64.float(), X64.float()
+        Y32 = torch.zeros((nblocks, N), dtype=torch.float32, device="cuda")
+        pA32 = ((lvl * pool + ai) * (n * n * 4) + A32.data_ptr()).reshape(-1).contiguous()
+        pX32 = xi * (N * 4) + X32.data_ptr()
+        pY32 = yi * (N * 4) + Y32.data_ptr()
+        for name, fm in (("f32_y32", None), ("f32_y32_tf32x3", "tf32x3")):
+            call = lambda: kmx.kronmult_xbatched(d, n, pA32, n, pX32, pY32, None, entries,
+                                                 dtype=torch.float32, form=fm)
+            ms = _events_time(torch, call, max(3, args.steps // 2), 2)
+            Y32.zero_()
+            call()
+            torch.cuda.synchronize()
+            Yd = Y32.double()
+            s = Yref.abs().amax(dim=1, keepdim=True).clamp_min(1e-300)
+            err = float((torch.linalg.vector_norm((Yd - Yref) / s, dim=1) /
+                         torch.linalg.vector_norm(Yref / s, dim=1).clamp_min(1e-300)).max())
+            res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                         "rel_err_vs_fp64_gpu": err}
+        del A32, X32, Y32
         out.append({"d": d, "n": n, "entries": entries, "forms": res,
                     "f32_speedup_vs_fp64_plain": round(res["plain"]["ms"] / res["f32"]["ms"], 2),
                     "f32_speedup_vs_fp64_chosen": round(res["split"]["ms"] / res["f32"]["ms"], 2),
