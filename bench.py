@@ -474,7 +474,7 @@ def run_ours(args):
                    "note": "FP64 as base-2^9 digits, exact FP16 tensor-core products "
                            "(mma.sync), double-float pass for handed-back entries"},
         "rel_err_chosen_vs_plain": err_vs_plain,
-        "roofline": roofline, "north_star_roofline": north,
+        "roofline": roofline, "fp64_roofline": north,
         "gpu_launches": args.steps, "gpu_launches_deterministic_per_step": 8, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
