@@ -36,7 +36,7 @@ typedef enum kmx_status {
   KMX_ERR_INVALID_ARG = 1,   /* d outside 1..6, n < 1, batch < 0, lda < n, ... */
   KMX_ERR_NULL_POINTER = 2,  /* a required array pointer is NULL */
   KMX_ERR_WORKSPACE = 3,     /* workspace missing or too small for an entry */
-  KMX_ERR_UNSUPPORTED = 4,   /* shape or option this build does not handle */
+  KMX_ERR_UNSUPPORTED = 4,   /* shape or option the library does not handle */
   KMX_ERR_CUDA = 5,          /* a CUDA runtime call failed (see kmx_last_cuda_error) */
   KMX_ERR_DEVICE = 6,        /* a kernel reported an error through the device status word */
   KMX_ERR_OVERLAP = 7        /* deterministic mode: Y blocks partially overlap (reported
@@ -353,7 +353,7 @@ double kmx_kron_flops(int d, const int* m, const int* n);
  * Used as the denominator of the compute roofline.  Synchronises the device. */
 int kmx_probe_fma_rate(int fp64, double* fma_per_second);
 
-/* Version string of this build. */
+/* Version string of the library. */
 const char* kmx_version(void);
 
 #ifdef __cplusplus

@@ -1,7 +1,7 @@
 /*
  * kron_oracle.c -- CPU oracle for the batched Kronecker mat-vec.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
  * smoke check and the CPU-baseline leg of the benchmark load it.  The CUDA
  * product path never links, loads or calls it.
  *
