@@ -624,3 +624,38 @@ def test_wide_forms_vs_fp64_oracle(kmx, oracle, in_dtype, d, n, acc):
     err = blockwise_rel_err(host(Yd), Yref)
     assert err <= 2e-6, err
     check_status(kmx)
+
+
+@pytest.mark.parametrize("form,acc", [("auto", "atomic"), ("digits", "atomic"),
+                                      ("auto", "deterministic")])
+def test_xbatched_cuda_graph_replay(kmx, form, acc):
+    """The xbatched call makes no host synchronisation in any form (the
+    digits form's second pass reads its count on the device; the
+    deterministic mode sorts on the device): after one warm-up call it
+    captures into a CUDA graph, and each replay adds the same contribution."""
+    rng = np.random.default_rng(33)
+    d, n, pool, nb, ne = 6, 4, 32, 24, 200
+    N = n ** d
+    Apool = dev(rng.standard_normal((d, pool, n, n)) / 2)
+    Xpool = dev(rng.standard_normal((nb, N)))
+    y_idx = rng.geometric(0.2, ne) % nb
+    x_idx = rng.integers(0, nb, ne)
+    a_idx = rng.integers(0, pool, (ne, d))
+    pA = kmx.pointer_array(Apool, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xpool, x_idx * N)
+    Y = torch.zeros((nb, N), dtype=torch.float64, device="cuda")
+    pY = kmx.pointer_array(Y, y_idx * N)
+    s = torch.cuda.Stream()
+    kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, ne, form=form, accumulate=acc, stream=s)
+    s.synchronize()
+    once = Y.clone()
+    Y.zero_()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, ne, form=form, accumulate=acc, stream=s)
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+    assert blockwise_rel_err(host(Y), 2 * host(once)) <= F64_TOL
