@@ -539,16 +539,16 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) 
     const bool zero_block = (sExp[MAXD] == 0);
     bool anyzero = zero_block;
     for (int l = 0; l < d; ++l) anyzero = anyzero || (sExp[l] == 0);
-    if (anyzero) {
-      // kron(...) X is exactly zero: nothing to add.
+    if (nonfinite) {
+      // Inf/NaN must propagate exactly as in FP64 (0 * Inf included): evaluate
+      // with the plain form on the same (double-sized) buffer.
+      double* sAd = reinterpret_cast<double*>(gbase);
+      sq_plain_entry<double, NN, GBUF>(p, en, sAd, reinterpret_cast<double*>(bufp), lt, G, g);
       group_sync(g, G);
       continue;
     }
-    if (nonfinite) {
-      // Inf/NaN must propagate exactly as in FP64: evaluate with the plain form
-      // on the same (double-sized) buffer.
-      double* sAd = reinterpret_cast<double*>(gbase);
-      sq_plain_entry<double, NN, GBUF>(p, en, sAd, reinterpret_cast<double*>(bufp), lt, G, g);
+    if (anyzero) {
+      // kron(...) X is exactly zero: nothing to add.
       group_sync(g, G);
       continue;
     }
@@ -632,6 +632,78 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) 
 // ---------------------------------------------------------------------------
 constexpr int GEN_MAXN = 64;
 
+// One entry of the generic plain kernel (also the Inf/NaN fallback of the
+// generic split kernel): factors into sA, modes through b0/b1, Y += result.
+template <typename T>
+__device__ __forceinline__ void gen_plain_entry(const Problem& p, const EntryPtrs<T>& en, T* sA,
+                                                T* b0, T* b1, int lt, int G, int g) {
+  const int d = p.d;
+  int aoff[MAXD + 1];
+  aoff[0] = 0;
+#pragma unroll
+  for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
+  const bool excl = p.y_exclusive != 0;
+  for (int l = 0; l < d; ++l) {
+    const int ml = p.m[l], nl = p.n[l];
+    for (int i = lt; i < ml * nl; i += G) {
+      const int a = i / nl, j = i - a * nl;
+      sA[aoff[l] + i] = p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                : en.A[l][a + (long long)j * en.ld[l]];
+    }
+  }
+  group_sync(g, G);
+  const T* src = en.X;
+  T* cur = b0;
+  unsigned outer = 1;
+  for (int k = 0; k < d; ++k) {
+    unsigned s = 1;
+    for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
+    const int mk = p.m[k], nk = p.n[k];
+    const T* Ak = sA + aoff[k];
+    const bool last = (k == d - 1);
+    if (!last && k > 0 && mk == nk) {
+      // square middle mode: in place on cur, one fiber per lane
+      const FastDiv fs(s);
+      const unsigned F = outer * s;
+      for (unsigned f = lt; f < F; f += G) {
+        const unsigned o = fs(f);
+        const unsigned r0 = f - o * s;
+        T* base = cur + (long long)o * nk * s + r0;
+        T v[GEN_MAXN];
+        for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
+        for (int a = 0; a < mk; ++a) {
+          T acc = Ak[a * nk] * v[0];
+          for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[j], acc);
+          base[(long long)a * s] = acc;
+        }
+      }
+    } else {
+      // out of place: one output element per lane
+      T* dst = last ? en.Y : ((k == 0) ? cur : (cur == b0 ? b1 : b0));
+      const FastDiv fs(s), fm((unsigned)mk);
+      const unsigned total = outer * (unsigned)mk * s;
+      for (unsigned q = lt; q < total; q += G) {
+        const unsigned t = fs(q);
+        const unsigned rr = q - t * s;
+        const unsigned o = fm(t);
+        const int a = (int)(t - o * (unsigned)mk);
+        const T* v = src + (long long)o * nk * s + rr;
+        T acc = Ak[a * nk] * v[0];
+        for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[(long long)j * s], acc);
+        if (last) {
+          y_accumulate(dst + q, acc, excl);
+        } else {
+          dst[q] = acc;
+        }
+      }
+      if (!last) cur = dst;
+    }
+    group_sync(g, G);
+    src = cur;
+    outer *= (unsigned)mk;
+  }
+}
+
 template <typename T, bool GBUF>
 __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -641,16 +713,13 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
   const int lt = threadIdx.x - g * G;
   if (g >= E) return;
   const int d = p.d;
-  int aoff[MAXD + 1];
-  aoff[0] = 0;
-#pragma unroll
-  for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
+  int nfac = 0;
+  for (int l = 0; l < d; ++l) nfac += p.m[l] * p.n[l];
   T* sA = reinterpret_cast<T*>(smem + (size_t)g * p.group_smem);
-  T* sb0 = sA + ((aoff[d] * sizeof(T) + 15) / 16 * 16) / sizeof(T);
+  T* sb0 = sA + ((nfac * sizeof(T) + 15) / 16 * 16) / sizeof(T);
   T* sb1 = sb0 + ((p.sxw * sizeof(T) + 15) / 16 * 16) / sizeof(T);
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
-  const bool excl = p.y_exclusive != 0;
   const long long count = launch_count(p);
   const long long obase = p.order_base ? (long long)*p.order_base : 0;
   for (long long e = slot0; e < count; e += step) {
@@ -668,63 +737,234 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
         continue;
       }
     }
+    gen_plain_entry<T>(p, en, sA, b0, b1, lt, G, g);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Generic path, split form: run-time (and rectangular) shapes in double-float,
+// the same mode structure as gen_plain_kernel.  X is split into the first
+// buffer (scaled by its block exponent), every factor by its own exponent and
+// stored transposed (column j of A_l contiguous), so the R rows one lane
+// accumulates are adjacent.  With two buffers every mode runs out of place: a
+// lane owns R outputs of one fiber (R independent two-sum chains sharing each
+// input load; R = 4 pays for long dot products, R = 1 keeps the registers and
+// so the occupancy of short ones).  With one buffer
+// (an entry too large for two on chip) the square modes of n <= GEN_SPLIT_MAXN
+// run in place, the lane holding its fiber.  The last mode widens to FP64 and
+// adds to Y.  Entries with Inf/NaN run the plain entry.
+// Shared memory per group: [factors as pairs][MAXD+2 exponents, 64 bytes]
+// [sxw pairs][sxw pairs when two buffers] (buffers in the workspace with GBUF).
+// ---------------------------------------------------------------------------
+constexpr int GEN_SPLIT_MAXN = 16;
+
+// A mode the generic split kernel can apply in place.
+__host__ __device__ inline bool gen_split_in_place(int m, int n) {
+  return m == n && n <= GEN_SPLIT_MAXN;
+}
+
+// R running double-float dot products sharing one input value per term.
+template <int R>
+struct DfRows {
+  float s[R], c[R];
+  __device__ __forceinline__ void first(const df* a, df v) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      s[r] = __fmul_rn(a[r].hi, v.hi);
+      float e = __fmaf_rn(a[r].hi, v.hi, -s[r]);
+      e = __fmaf_rn(a[r].hi, v.lo, e);
+      c[r] = __fmaf_rn(a[r].lo, v.hi, e);
+    }
+  }
+  __device__ __forceinline__ void add(const df* a, df v) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float pr = __fmul_rn(a[r].hi, v.hi);
+      float e = __fmaf_rn(a[r].hi, v.hi, -pr);
+      e = __fmaf_rn(a[r].hi, v.lo, e);
+      e = __fmaf_rn(a[r].lo, v.hi, e);
+      float t, te;
+      two_sum(s[r], pr, t, te);
+      s[r] = t;
+      c[r] = __fadd_rn(c[r], __fadd_rn(te, e));
+    }
+  }
+  __device__ __forceinline__ df get(int r) const {
+    df o;
+    o.hi = __fadd_rn(s[r], c[r]);
+    o.lo = __fsub_rn(c[r], __fsub_rn(o.hi, s[r]));
+    return o;
+  }
+};
+
+template <bool GBUF, int R>
+__global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int G = p.group_threads;
+  const int E = p.groups_per_cta;
+  const int g = threadIdx.x / G;
+  const int lt = threadIdx.x - g * G;
+  if (g >= E) return;
+  const int d = p.d;
+  int aoff[MAXD + 1];
+  aoff[0] = 0;
+#pragma unroll
+  for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
+  unsigned char* gbase = smem + (size_t)g * p.group_smem;
+  df* sA = reinterpret_cast<df*>(gbase);
+  const size_t fac_bytes = ((size_t)aoff[d] * 8 + 15) / 16 * 16;
+  int* sExp = reinterpret_cast<int*>(gbase + fac_bytes);  // MAXD + 2 ints (64 bytes)
+  unsigned char* braw = gbase + fac_bytes + 64;
+  const size_t bbytes = ((size_t)p.sxw * 8 + 15) / 16 * 16;
+  const bool two = GBUF || (size_t)p.group_smem >= fac_bytes + 64 + 2 * bbytes;
+  const long long slot0 = (long long)blockIdx.x * E + g;
+  const long long step = (long long)gridDim.x * E;
+  const bool excl = p.y_exclusive != 0;
+  const long long count = launch_count(p);
+  const long long obase = p.order_base ? (long long)*p.order_base : 0;
+  const long long Nx = p.Nx;
+  for (long long e = slot0; e < count; e += step) {
+    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
+    EntryPtrs<double> en;
+    if (!resolve_entry<double>(p, entry, en)) {
+      if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    double *w0 = reinterpret_cast<double*>(braw), *w1 = reinterpret_cast<double*>(braw + bbytes);
+    if (GBUF) {
+      if (!workspace<double>(p, entry, slot0, w0, w1)) {
+        if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
+        continue;
+      }
+    }
+    // --- scales: max exponent field per factor and of X ---
+    if (lt < MAXD + 2) sExp[lt] = 0;
+    group_sync(g, G);
+    for (int l = 0; l < d; ++l) {
+      const int ml = p.m[l], nl = p.n[l];
+      int em = 0;
+      for (int i = lt; i < ml * nl; i += G) {
+        const int a = i / nl, j = i - a * nl;
+        em = max(em, exp_field(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                       : en.A[l][a + (long long)j * en.ld[l]]));
+      }
+      if (em > 0) atomicMax(&sExp[l], em);
+    }
+    {
+      int ex = 0;
+      for (long long i = lt; i < Nx; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
+      if (ex > 0) atomicMax(&sExp[MAXD], ex);
+    }
+    group_sync(g, G);
+    int nonfinite = (sExp[MAXD] == 2047);
+    int escale = sExp[MAXD] - 1023;
+    bool anyzero = sExp[MAXD] == 0;
+    for (int l = 0; l < d; ++l) {
+      nonfinite |= (sExp[l] == 2047);
+      escale += sExp[l] - 1023;
+      anyzero = anyzero || sExp[l] == 0;
+    }
+    if (nonfinite) {
+      // Inf/NaN propagate exactly as in FP64 (0 * Inf included): the plain
+      // entry on the same memory
+      gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
+      group_sync(g, G);
+      continue;
+    }
+    if (anyzero) {  // kron(...) X is exactly zero
+      group_sync(g, G);
+      continue;
+    }
+    // --- factors (transposed: sA[aoff[l] + j*m_l + a] = A_l(a, j)) and X, split ---
     for (int l = 0; l < d; ++l) {
       const int ml = p.m[l], nl = p.n[l];
       for (int i = lt; i < ml * nl; i += G) {
-        const int a = i / nl, j = i - a * nl;
-        sA[aoff[l] + i] = p.trans ? en.A[l][j + (long long)a * en.ld[l]]
-                                  : en.A[l][a + (long long)j * en.ld[l]];
+        const int j = i / ml, a = i - j * ml;
+        sA[aoff[l] + i] = split_scaled(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                               : en.A[l][a + (long long)j * en.ld[l]],
+                                       sExp[l]);
       }
     }
+    df* b0 = reinterpret_cast<df*>(w0);
+    df* b1 = reinterpret_cast<df*>(w1);
+    const int ex = sExp[MAXD];
+    for (long long i = lt; i < Nx; i += G) b0[i] = split_scaled(__ldg(en.X + i), ex);
     group_sync(g, G);
-    const T* src = en.X;
-    T* cur = b0;
+    df* cur = b0;
     unsigned outer = 1;
     for (int k = 0; k < d; ++k) {
       unsigned s = 1;
       for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
       const int mk = p.m[k], nk = p.n[k];
-      const T* Ak = sA + aoff[k];
+      const df* At = sA + aoff[k];
       const bool last = (k == d - 1);
-      if (!last && k > 0 && mk == nk) {
-        // square middle mode: in place on cur, one fiber per lane
+      const int nb = (mk + R - 1) / R;
+      if (!last && !two && gen_split_in_place(mk, nk)) {
+        // one buffer: in place on cur, one fiber per lane
         const FastDiv fs(s);
         const unsigned F = outer * s;
         for (unsigned f = lt; f < F; f += G) {
           const unsigned o = fs(f);
           const unsigned r0 = f - o * s;
-          T* base = cur + (long long)o * nk * s + r0;
-          T v[GEN_MAXN];
+          df* base = cur + (long long)o * nk * s + r0;
+          df v[GEN_SPLIT_MAXN];
           for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
-          for (int a = 0; a < mk; ++a) {
-            T acc = Ak[a * nk] * v[0];
-            for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[j], acc);
-            base[(long long)a * s] = acc;
+          for (int ab = 0; ab < nb; ++ab) {
+            const int a0 = ab * R;
+            df av[R];
+            DfRows<R> acc;
+#pragma unroll
+            for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
+            acc.first(av, v[0]);
+            for (int j = 1; j < nk; ++j) {
+#pragma unroll
+              for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
+              acc.add(av, v[j]);
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+              if (a0 + r < mk) base[(long long)(a0 + r) * s] = acc.get(r);
           }
         }
       } else {
-        // out of place: one output element per lane
-        T* dst = last ? en.Y : ((k == 0) ? cur : (cur == b0 ? b1 : b0));
-        const FastDiv fs(s), fm((unsigned)mk);
-        const unsigned total = outer * (unsigned)mk * s;
+        // out of place: a lane owns rows a0..a0+R-1 of one fiber
+        df* dst = last ? nullptr : (cur == b0 ? b1 : b0);
+        const FastDiv fs(s), fb((unsigned)nb);
+        const unsigned total = outer * (unsigned)nb * s;
         for (unsigned q = lt; q < total; q += G) {
           const unsigned t = fs(q);
           const unsigned rr = q - t * s;
-          const unsigned o = fm(t);
-          const int a = (int)(t - o * (unsigned)mk);
-          const T* v = src + (long long)o * nk * s + rr;
-          T acc = Ak[a * nk] * v[0];
-          for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[(long long)j * s], acc);
-          if (last) {
-            y_accumulate(dst + q, acc, excl);
-          } else {
-            dst[q] = acc;
+          const unsigned o = fb(t);
+          const int a0 = (int)(t - o * (unsigned)nb) * R;
+          const df* v = cur + (long long)o * nk * s + rr;
+          df av[R];
+          DfRows<R> acc;
+#pragma unroll
+          for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
+          acc.first(av, v[0]);
+          for (int j = 1; j < nk; ++j) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
+            acc.add(av, v[(long long)j * s]);
+          }
+          const long long obase_q = ((long long)o * mk + a0) * s + rr;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            if (a0 + r < mk) {
+              const df o2 = acc.get(r);
+              if (last) {
+                const double y =
+                    f32_to_f64_scaled(o2.hi, escale) + f32_to_f64_scaled(o2.lo, escale);
+                y_accumulate(en.Y + obase_q + (long long)r * s, y, excl);
+              } else {
+                dst[obase_q + (long long)r * s] = o2;
+              }
+            }
           }
         }
         if (!last) cur = dst;
       }
       group_sync(g, G);
-      src = cur;
       outer *= (unsigned)mk;
     }
   }

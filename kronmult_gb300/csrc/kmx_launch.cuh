@@ -191,6 +191,22 @@ size_t gen_group_smem(const Problem& p, bool gbuf) {
   return head + (is_square(p) ? 1 : 2) * align16((size_t)p.sxw * sizeof(T));
 }
 
+// Generic split kernel: [factors as pairs][MAXD+2 exponents, 64 bytes]
+// [two buffers: every mode out of place], or one buffer when two would not
+// fit on chip and every mode but the last can run in place.  X itself is
+// split into the first buffer, so d = 1 needs one too.
+inline size_t gen_split_group_smem(const Problem& p, bool gbuf, size_t limit) {
+  size_t fac = 0;
+  for (int l = 0; l < p.d; ++l) fac += (size_t)p.m[l] * p.n[l];
+  const size_t head = align16(fac * 8) + 64;
+  if (gbuf) return head;
+  const size_t b = align16((size_t)p.sxw * 8);
+  bool one_ok = true;
+  for (int k = 0; k + 1 < p.d; ++k) one_ok = one_ok && gen_split_in_place(p.m[k], p.n[k]);
+  if (head + 2 * b <= limit || !one_ok) return head + 2 * b;
+  return head + b;
+}
+
 // Launch one forward pass over p.count entries.  Returns cudaSuccess, or the
 // CUDA error of the launch; cudaErrorInvalidValue when the shape needs a
 // global workspace that p does not provide.
@@ -217,21 +233,42 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
     return cudaErrorNotSupported;  // register-tiled shapes only (handled above)
   } else {
   const bool spec = square && pick_sq<T, FORM, false>(nn) != nullptr;
-  // FORM_SPLIT exists for specialised square shapes only; others run plain.
-  if (FORM == FORM_SPLIT && !spec) return cudaErrorNotSupported;
-
+  auto group_smem = [&](bool gb) -> size_t {
+    if (spec) return sq_group_smem<T, FORM>(p, gb);
+    if constexpr (FORM == FORM_SPLIT) return gen_split_group_smem(p, gb, di.max_smem_optin);
+    return gen_group_smem<T>(p, gb);
+  };
   bool gbuf = false;
-  size_t gsm = spec ? sq_group_smem<T, FORM>(p, false) : gen_group_smem<T>(p, false);
+  size_t gsm = group_smem(false);
   if (gsm > (size_t)di.max_smem_optin) {
     gbuf = true;
-    gsm = spec ? sq_group_smem<T, FORM>(p, true) : gen_group_smem<T>(p, true);
+    gsm = group_smem(true);
     if (p.wmode == 0 || p.nslots <= 0) return cudaErrorInvalidValue;
   }
-  const void* func = spec ? (gbuf ? pick_sq<T, FORM, true>(nn) : pick_sq<T, FORM, false>(nn))
-                          : (gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true>)
-                                  : reinterpret_cast<const void*>(&gen_plain_kernel<T, false>));
+  const void* func = nullptr;
+  if (spec) {
+    func = gbuf ? pick_sq<T, FORM, true>(nn) : pick_sq<T, FORM, false>(nn);
+  } else if constexpr (FORM == FORM_SPLIT) {
+    // four rows per lane once some dot product has 16 or more terms
+    int nmax = 0;
+    for (int l = 0; l < p.d; ++l) nmax = p.n[l] > nmax ? p.n[l] : nmax;
+    if (nmax >= 16) {
+      func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 4>)
+                  : reinterpret_cast<const void*>(&gen_split_kernel<false, 4>);
+    } else {
+      func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 1>)
+                  : reinterpret_cast<const void*>(&gen_split_kernel<false, 1>);
+    }
+  } else {
+    func = gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true>)
+                : reinterpret_cast<const void*>(&gen_plain_kernel<T, false>);
+  }
 
   int G = hint.group_threads > 0 ? hint.group_threads : default_group_threads(p.Nx > p.Ny ? p.Nx : p.Ny, spec ? nn : 1);
+  // a generic split entry that holds more than half of the shared memory runs
+  // alone on its SM: give it every thread
+  if (FORM == FORM_SPLIT && !spec && hint.group_threads <= 0 && 2 * gsm > (size_t)di.max_smem_optin)
+    G = MAX_THREADS;
   if (G > MAX_THREADS) G = MAX_THREADS;
   G = round_up(G, 32);
   int E = hint.groups_per_cta > 0 ? hint.groups_per_cta : (256 / G > 0 ? 256 / G : 1);

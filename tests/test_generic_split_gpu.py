@@ -1,0 +1,201 @@
+"""GPU parity of the generic split (double-float) kernel: rectangular factors
+(the reference's vbatched, kronmult_vbatched.hpp:19-248) and square n without
+a compile-time specialisation, against the oracle.  Every call goes through
+the C ABI.
+
+Tolerance: normwise relative error per Y block <= 1e-13 (FP64 forms).
+"""
+import numpy as np
+import pytest
+
+from tests.common import blockwise_rel_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+F64_TOL = 1e-13
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def check_status(kmx):
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+
+
+def kernels_of(fn):
+    """Names of the CUDA kernels fn launches (None when the profiler sees no
+    device activity on this build of torch)."""
+    from torch.profiler import ProfilerActivity, profile
+
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        fn()
+        torch.cuda.synchronize()
+    names = [e.name for e in prof.events() if e.device_type == torch.autograd.DeviceType.CUDA]
+    return names or None
+
+
+def vb_case(seed, d, m, nn, batch, scale_exp=0, y0=True):
+    rng = np.random.default_rng(seed)
+    Nx, Ny = int(np.prod(nn)), int(np.prod(m))
+    fsz = [m[l] * nn[l] for l in range(d)]
+    A = rng.standard_normal(batch * sum(fsz))
+    offs, o = [], 0
+    for b in range(batch):
+        for l in range(d):
+            if scale_exp:
+                A[o:o + fsz[l]] *= 10.0 ** rng.integers(-scale_exp, scale_exp + 1)
+            offs.append(o)
+            o += fsz[l]
+    X = rng.standard_normal((batch, Nx))
+    if scale_exp:
+        X *= 10.0 ** rng.integers(-2 * scale_exp, 2 * scale_exp + 1, (batch, 1))
+    Y0 = rng.uniform(-1, 1, (batch, Ny)) if y0 else np.zeros((batch, Ny))
+    return A, offs, X, Y0
+
+
+def run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, form, wslots=None):
+    batch, Nx = X.shape
+    Ny = Y0.shape[1]
+    sxw = oracle.size_xw(d, m, nn)
+    Yref = Y0.copy()
+    oracle.vbatched(d, m, nn, A, offs, X, [b * Nx for b in range(batch)], Yref,
+                    [b * Ny for b in range(batch)], np.zeros(2 * sxw * batch))
+    Ad, Xd, Yd = dev(A), dev(X), dev(Y0)
+    nslots = batch if wslots is None else wslots
+    W = torch.zeros(2 * sxw * nslots, dtype=torch.float64, device="cuda")
+
+    def call():
+        kmx.kronmult_vbatched(d, m, nn, kmx.pointer_array(Ad, offs),
+                              kmx.pointer_array(Xd, [b * Nx for b in range(batch)]),
+                              kmx.pointer_array(Yd, [b * Ny for b in range(batch)]), W, None,
+                              batch, form=form)
+
+    return call, Yd, Yref
+
+
+RECT = [
+    (1, [5], [3]),
+    (2, [3, 7], [6, 2]),
+    (3, [4, 5, 6], [6, 5, 4]),
+    (3, [2, 9, 3], [9, 2, 9]),
+    (4, [3, 4, 3, 4], [4, 3, 4, 3]),
+    (5, [2, 3, 4, 3, 2], [3, 2, 3, 4, 3]),
+    (6, [4, 3, 4, 3, 4, 3], [3, 4, 3, 4, 3, 4]),
+    (6, [2, 2, 3, 3, 2, 2], [3, 3, 2, 2, 3, 3]),
+    (4, [17, 5, 17, 5], [5, 17, 5, 17]),
+]
+
+
+@pytest.mark.parametrize("d,m,nn", RECT)
+def test_generic_split_rectangular_vs_oracle(kmx, oracle, d, m, nn):
+    """Rectangular factors in double-float, accumulated into a nonzero Y."""
+    A, offs, X, Y0 = vb_case(31 + d, d, m, nn, batch=6)
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, "split")
+    names = kernels_of(call)
+    if names is not None:
+        assert any("gen_split_kernel" in k for k in names), names
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("d,n", [(3, 9), (4, 11), (2, 13), (3, 17), (2, 20), (3, 1), (4, 10)])
+def test_generic_split_unspecialised_square_vs_oracle(kmx, oracle, d, n):
+    """Square n without a compiled specialisation: n <= 16 runs in place, n > 16
+    through the second buffer."""
+    rng = np.random.default_rng(100 * d + n)
+    N = n ** d
+    batch = 4
+    A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+    X = rng.standard_normal((batch, N))
+    Y0 = rng.uniform(-1, 1, (batch, N))
+    Yref = Y0.copy()
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Xd, Yd, Ad = dev(X), dev(Y0), dev(A)
+
+    def call():
+        kmx.kronmult_batched(d, n, Ad, Xd, Yd, None, batch, form="split")
+
+    names = kernels_of(call)
+    if names is not None:
+        assert any("gen_split_kernel" in k for k in names), names
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+def test_generic_split_global_workspace(kmx, oracle):
+    """d=5 with 8x7 / 7x8 factors: one entry exceeds shared memory, so the
+    split kernel keeps its pairs in the caller's workspace slots (two slots
+    for three entries: slots are reused)."""
+    d, m, nn = 5, [8, 7, 8, 7, 8], [7, 8, 7, 8, 8]
+    A, offs, X, Y0 = vb_case(41, d, m, nn, batch=3)
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, "split", wslots=2)
+    names = kernels_of(call)
+    if names is not None:
+        assert any("gen_split_kernel" in k for k in names), names
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("d,m,nn", [RECT[2], RECT[6], RECT[8]])
+def test_generic_split_extreme_magnitudes(kmx, oracle, d, m, nn):
+    """Factors scaled by 1e-30..1e30 and X by 1e-60..1e60: per-entry power-of-
+    two scaling keeps the FP32 carriers in range."""
+    A, offs, X, _ = vb_case(51, d, m, nn, batch=5, scale_exp=30, y0=False)
+    Y0 = np.zeros((X.shape[0], int(np.prod(m))))
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, "split")
+    call()
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+def test_generic_split_nonfinite_like_fp64(kmx, oracle):
+    """Inf/NaN in X or a factor: those entries run the FP64 arithmetic, so
+    Inf/NaN land where FP64 puts them; the other entries stay in tolerance."""
+    d, m, nn = 4, [3, 4, 3, 4], [4, 3, 4, 3]
+    A, offs, X, _ = vb_case(61, d, m, nn, batch=4, y0=False)
+    X[1, 17] = np.inf
+    A[offs[2 * d + 2] + 3] = np.nan
+    # entry 3: an all-zero factor times an Inf in X gives NaN, as in FP64
+    A[offs[3 * d + 1]:offs[3 * d + 1] + m[1] * nn[1]] = 0.0
+    X[3, 5] = -np.inf
+    Y0 = np.zeros((4, int(np.prod(m))))
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, "split")
+    call()
+    y = host(Yd)
+    assert np.isnan(Yref[3]).any()
+    assert np.array_equal(np.isnan(y), np.isnan(Yref))
+    assert np.array_equal(np.isinf(y), np.isinf(Yref))
+    fin = np.isfinite(Yref).all(axis=1)
+    assert fin.sum() == 1
+    assert blockwise_rel_err(y[fin], Yref[fin]) <= F64_TOL
+    check_status(kmx)
+
+
+def test_generic_split_zero_factor_adds_nothing(kmx, oracle):
+    """An all-zero factor or X block contributes exactly zero (Y unchanged)."""
+    d, m, nn = 3, [4, 5, 6], [6, 5, 4]
+    A, offs, X, Y0 = vb_case(71, d, m, nn, batch=3)
+    A[offs[1]:offs[1] + m[1] * nn[1]] = 0.0  # entry 0, factor 1
+    X[2] = 0.0
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, "split")
+    call()
+    y = host(Yd)
+    assert np.array_equal(y[0], Y0[0]) and np.array_equal(y[2], Y0[2])
+    assert blockwise_rel_err(y[1:2], Yref[1:2]) <= F64_TOL
+    check_status(kmx)

@@ -394,6 +394,32 @@ def test_nonfinite_inputs_propagate_like_fp64(kmx, oracle, form):
     assert blockwise_rel_err(y[fin], Yref[fin]) <= F64_TOL
 
 
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d,n", [(6, 4), (3, 8), (2, 16), (4, 5)])
+def test_zero_factor_times_inf_is_nan(kmx, oracle, form, d, n):
+    """An all-zero factor with an Inf in X gives NaN (0 * Inf), as in FP64: the
+    split and digits forms must not take their all-zero shortcut first."""
+    rng = np.random.default_rng(23)
+    N = n ** d
+    batch = 3
+    A = rng.standard_normal((batch, d, n, n))
+    X = rng.standard_normal((batch, N))
+    A[1, d // 2] = 0.0
+    X[1, N // 3] = np.inf
+    A[2, 0] = 0.0  # all-zero factor, finite X: contributes exactly zero
+    Y0 = rng.uniform(-1, 1, (batch, N))
+    Yref = Y0.copy()
+    oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
+    Yd = dev(Y0)
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form=form)
+    y = host(Yd)
+    assert np.isnan(Yref[1]).any()
+    assert np.array_equal(np.isnan(y), np.isnan(Yref))
+    assert np.array_equal(np.isinf(y), np.isinf(Yref))
+    assert np.array_equal(y[2], Y0[2])
+    assert blockwise_rel_err(y[0:1], Yref[0:1]) <= F64_TOL
+
+
 # ---------------------------------------------------------------------------
 # deterministic (sorted-segment) accumulation
 # ---------------------------------------------------------------------------
