@@ -47,7 +47,9 @@ typedef enum kmx_status {
  * entry points (the _f32 functions and kmx_kronmult_xbatched_wide): FP32
  * fused multiply-add unless TF32X3 is asked for. */
 typedef enum kmx_form {
-  KMX_FORM_AUTO = 0,   /* per-(d,n) choice from the tuning table */
+  KMX_FORM_AUTO = 0,   /* square shapes: per-(d,n) choice from the tuning table;
+                          other shapes: SPLIT once an X or Y block has 512 or more
+                          elements, PLAIN below */
   KMX_FORM_PLAIN = 1,  /* native FP64 fused multiply-add */
   KMX_FORM_SPLIT = 2,  /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
                           ~2^-47 relative per operation, FP64 in and out */

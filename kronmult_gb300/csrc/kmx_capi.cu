@@ -224,7 +224,11 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     int form = o.form;
     if (form == KMX_FORM_AUTO) {
       const int t = sq ? tuned_form(p.d, p.n[0]) : 0;
-      form = t ? t : ((sq && spec_n) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
+      // double-float wherever it measured faster: the specialised square
+      // kernels, and the generic kernel once an entry has 512 elements
+      // (below that its per-entry scaling costs more than FP64 does)
+      const bool gen_split = p.Nx >= 512 || p.Ny >= 512;
+      form = t ? t : (((sq && spec_n) || gen_split) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
     }
     if (h.engine == 0 && sq)
       h.engine = tuned_engine((form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1, p.d,

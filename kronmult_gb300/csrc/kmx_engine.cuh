@@ -748,11 +748,12 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
 // stored transposed (column j of A_l contiguous), so the R rows one lane
 // accumulates are adjacent.  With two buffers every mode runs out of place: a
 // lane owns R outputs of one fiber (R independent two-sum chains sharing each
-// input load; R = 4 pays for long dot products, R = 1 keeps the registers and
-// so the occupancy of short ones).  With one buffer
-// (an entry too large for two on chip) the square modes of n <= GEN_SPLIT_MAXN
-// run in place, the lane holding its fiber.  The last mode widens to FP64 and
-// adds to Y.  Entries with Inf/NaN run the plain entry.
+// input load; the launcher picks R = 4 for large entries and R = 2 for small
+// ones, where the extra registers cost more occupancy than they win).  With
+// one buffer (an entry too large for two on chip, or a large one whose modes
+// but the last are all square with n <= GEN_SPLIT_MAXN) those modes run in
+// place, the lane holding its fiber.  The last mode widens to FP64 and adds
+// to Y.  Entries with Inf/NaN run the plain entry.
 // Shared memory per group: [factors as pairs][MAXD+2 exponents, 64 bytes]
 // [sxw pairs][sxw pairs when two buffers] (buffers in the workspace with GBUF).
 // ---------------------------------------------------------------------------

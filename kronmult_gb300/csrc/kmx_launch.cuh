@@ -191,10 +191,16 @@ size_t gen_group_smem(const Problem& p, bool gbuf) {
   return head + (is_square(p) ? 1 : 2) * align16((size_t)p.sxw * sizeof(T));
 }
 
-// Generic split kernel: [factors as pairs][MAXD+2 exponents, 64 bytes]
-// [two buffers: every mode out of place], or one buffer when two would not
-// fit on chip and every mode but the last can run in place.  X itself is
-// split into the first buffer, so d = 1 needs one too.
+// Generic split kernel.  Rows per lane and buffers, as measured on GB300
+// (d = 2..6, n = 3..32): entries of 4096 or more elements take four rows per
+// lane and, where every mode but the last is square with n <= 16 and one
+// buffer fits, work in place (the fiber a lane holds is reused for four
+// rows); smaller entries take two rows per lane and ping-pong between two
+// buffers.
+inline bool gen_split_wide(const Problem& p) { return p.Nx >= 4096 || p.Ny >= 4096; }
+
+// [factors as pairs][MAXD+2 exponents, 64 bytes][one or two buffers].  X
+// itself is split into the first buffer, so d = 1 needs one too.
 inline size_t gen_split_group_smem(const Problem& p, bool gbuf, size_t limit) {
   size_t fac = 0;
   for (int l = 0; l < p.d; ++l) fac += (size_t)p.m[l] * p.n[l];
@@ -203,8 +209,8 @@ inline size_t gen_split_group_smem(const Problem& p, bool gbuf, size_t limit) {
   const size_t b = align16((size_t)p.sxw * 8);
   bool one_ok = true;
   for (int k = 0; k + 1 < p.d; ++k) one_ok = one_ok && gen_split_in_place(p.m[k], p.n[k]);
-  if (head + 2 * b <= limit || !one_ok) return head + 2 * b;
-  return head + b;
+  if (one_ok && (gen_split_wide(p) || head + 2 * b > limit)) return head + b;
+  return head + 2 * b;
 }
 
 // Launch one forward pass over p.count entries.  Returns cudaSuccess, or the
@@ -249,15 +255,12 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   if (spec) {
     func = gbuf ? pick_sq<T, FORM, true>(nn) : pick_sq<T, FORM, false>(nn);
   } else if constexpr (FORM == FORM_SPLIT) {
-    // four rows per lane once some dot product has 16 or more terms
-    int nmax = 0;
-    for (int l = 0; l < p.d; ++l) nmax = p.n[l] > nmax ? p.n[l] : nmax;
-    if (nmax >= 16) {
+    if (gen_split_wide(p)) {
       func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 4>)
                   : reinterpret_cast<const void*>(&gen_split_kernel<false, 4>);
     } else {
-      func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 1>)
-                  : reinterpret_cast<const void*>(&gen_split_kernel<false, 1>);
+      func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 2>)
+                  : reinterpret_cast<const void*>(&gen_split_kernel<false, 2>);
     }
   } else {
     func = gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true>)

@@ -199,3 +199,20 @@ def test_generic_split_zero_factor_adds_nothing(kmx, oracle):
     assert np.array_equal(y[0], Y0[0]) and np.array_equal(y[2], Y0[2])
     assert blockwise_rel_err(y[1:2], Yref[1:2]) <= F64_TOL
     check_status(kmx)
+
+
+@pytest.mark.parametrize("d,m,nn,kernel", [
+    (3, [10, 12, 10], [12, 10, 12], "gen_split_kernel"),
+    (2, [32, 24], [24, 32], "gen_split_kernel"),
+    (2, [6, 7], [7, 6], "gen_plain_kernel"),
+])
+def test_auto_form_for_generic_shapes(kmx, oracle, d, m, nn, kernel):
+    """The automatic form takes double-float for entries of 512 or more
+    elements and FP64 below (where the per-entry scaling costs more)."""
+    A, offs, X, Y0 = vb_case(81, d, m, nn, batch=4)
+    call, Yd, Yref = run_vb(kmx, oracle, d, m, nn, A, offs, X, Y0, None)
+    names = kernels_of(call)
+    if names is not None:
+        assert any(kernel in k for k in names), names
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
