@@ -524,10 +524,16 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) 
       }
       int ex = 0;
       for (int i = lt; i < N; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
+      // one shared atomic per warp (groups are whole warps)
 #pragma unroll
-      for (int l = 0; l < MAXD; ++l)
-        if (l < d && emax[l] > 0) atomicMax(&sExp[l], emax[l]);
-      if (ex > 0) atomicMax(&sExp[MAXD], ex);
+      for (int l = 0; l < MAXD; ++l) {
+        if (l < d) {
+          const int m = __reduce_max_sync(0xffffffffu, emax[l]);
+          if ((lt & 31) == 0 && m > 0) atomicMax(&sExp[l], m);
+        }
+      }
+      ex = __reduce_max_sync(0xffffffffu, ex);
+      if ((lt & 31) == 0 && ex > 0) atomicMax(&sExp[MAXD], ex);
     }
     group_sync(g, G);
     int nonfinite = (sExp[MAXD] == 2047);
@@ -849,12 +855,14 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
         em = max(em, exp_field(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
                                        : en.A[l][a + (long long)j * en.ld[l]]));
       }
-      if (em > 0) atomicMax(&sExp[l], em);
+      em = __reduce_max_sync(0xffffffffu, em);  // one shared atomic per warp
+      if ((lt & 31) == 0 && em > 0) atomicMax(&sExp[l], em);
     }
     {
       int ex = 0;
       for (long long i = lt; i < Nx; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
-      if (ex > 0) atomicMax(&sExp[MAXD], ex);
+      ex = __reduce_max_sync(0xffffffffu, ex);
+      if ((lt & 31) == 0 && ex > 0) atomicMax(&sExp[MAXD], ex);
     }
     group_sync(g, G);
     int nonfinite = (sExp[MAXD] == 2047);

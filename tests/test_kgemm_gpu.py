@@ -138,6 +138,35 @@ def test_kgemm_random_sweep_vs_oracle(kmx, oracle, trans, tag):
         assert err <= tol, (mm, nn, kk, err)
 
 
+@pytest.mark.parametrize("beta", [0.0, 1.0, -0.4])
+def test_kgemm_f32_dense_streaming_vs_oracle(kmx, oracle, beta):
+    """FP32 nn with dense B and C (ldB == kk, ldC == mm) and a long column
+    dimension: the chunk's columns move through shared memory as contiguous
+    runs.  Ragged last chunks, kk = 1, and (beta == 1) every entry adding into
+    one shared C."""
+    rng = np.random.default_rng(12)
+    T = np.float32
+    for (mm, nn, kk) in [(4, 1024, 4), (5, 3125, 5), (16, 4096, 16), (6, 7776, 6), (1, 4097, 1),
+                         (7, 2000, 3), (16, 300, 16), (3, 2187, 3), (12, 700, 9)]:
+        batch = 4
+        A = rng.standard_normal(batch * mm * kk).astype(T)
+        B = rng.standard_normal(batch * kk * nn).astype(T)
+        shared = beta == 1.0
+        C = rng.standard_normal((1 if shared else batch) * mm * nn).astype(T)
+        aoff = [i * mm * kk for i in range(batch)]
+        boff = [i * kk * nn for i in range(batch)]
+        coff = [0] * batch if shared else [i * mm * nn for i in range(batch)]
+        ref = C.copy()
+        oracle.kgemm_batched("nn", mm, nn, kk, 0.7, A, aoff, [mm] * batch, B, boff, [kk] * batch,
+                             beta, ref, coff, [mm] * batch)
+        got = _run_gpu(kmx, "nn", A, aoff, [mm] * batch, B, boff, [kk] * batch, C, coff,
+                       [mm] * batch, mm, nn, kk, 0.7, beta)
+        rows = 1 if shared else batch
+        err = blockwise_rel_err(got.astype(np.float64).reshape(rows, -1),
+                                ref.astype(np.float64).reshape(rows, -1))
+        assert err <= F32_NORM_TOL, (mm, nn, kk, beta, err)
+
+
 def test_kgemm_kk_zero_scales_c(kmx):
     """kk == 0: the product is empty and C becomes beta*C (beta == 0: zero)."""
     C = np.arange(1, 13, dtype=np.float64)
