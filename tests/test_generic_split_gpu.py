@@ -216,3 +216,56 @@ def test_auto_form_for_generic_shapes(kmx, oracle, d, m, nn, kernel):
         assert any(kernel in k for k in names), names
     assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
     check_status(kmx)
+
+
+@pytest.mark.parametrize("form", ["split", "plain"])
+@pytest.mark.parametrize("d,m,nn", [RECT[2], RECT[5], RECT[8]])
+def test_generic_transpose_option_rectangular(kmx, oracle, d, m, nn, form):
+    """transpose=True applies A_l^T (n_l x m_l) from factors stored m_l x n_l:
+    checked against the oracle on the explicitly transposed factors."""
+    rng = np.random.default_rng(91 + d)
+    batch = 4
+    # applied operator l is n_l x m_l: X blocks have prod(m) elements, Y blocks prod(n)
+    Nx, Ny = int(np.prod(m)), int(np.prod(nn))
+    fsz = [m[l] * nn[l] for l in range(d)]
+    F = rng.standard_normal(batch * sum(fsz))          # stored m_l x n_l, column-major
+    G = np.empty_like(F)                               # the transposes, n_l x m_l
+    offs, o = [], 0
+    for b in range(batch):
+        for l in range(d):
+            blk = F[o:o + fsz[l]].reshape(nn[l], m[l]).T   # (m_l, n_l) matrix
+            G[o:o + fsz[l]] = blk.T.reshape(-1, order="F")
+            offs.append(o)
+            o += fsz[l]
+    X = rng.standard_normal((batch, Nx))
+    Y0 = rng.uniform(-1, 1, (batch, Ny))
+    Yref = Y0.copy()
+    sxw = oracle.size_xw(d, nn, m)
+    oracle.vbatched(d, nn, m, G, offs, X, [b * Nx for b in range(batch)], Yref,
+                    [b * Ny for b in range(batch)], np.zeros(2 * sxw * batch))
+    Fd, Xd, Yd = dev(F), dev(X), dev(Y0)
+    W = torch.zeros(2 * sxw * batch, dtype=torch.float64, device="cuda")
+    kmx.kronmult_vbatched(d, m, nn, kmx.pointer_array(Fd, offs),
+                          kmx.pointer_array(Xd, [b * Nx for b in range(batch)]),
+                          kmx.pointer_array(Yd, [b * Ny for b in range(batch)]), W, None, batch,
+                          form=form, transpose=True)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
+
+
+@pytest.mark.parametrize("d,n", [(3, 9), (4, 10), (2, 20)])
+def test_generic_split_transpose_option_square(kmx, oracle, d, n):
+    """transpose=True on square unspecialised n against the oracle on A^T."""
+    rng = np.random.default_rng(95 + n)
+    N = n ** d
+    batch = 3
+    A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+    X = rng.standard_normal((batch, N))
+    Y0 = rng.uniform(-1, 1, (batch, N))
+    Yref = Y0.copy()
+    oracle.batched(d, n, np.ascontiguousarray(np.swapaxes(A, 2, 3)), X.copy(), Yref,
+                   np.zeros_like(X), batch)
+    Yd = dev(Y0)
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", transpose=True)
+    assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
+    check_status(kmx)
