@@ -875,10 +875,68 @@ def run_rect(args):
         out.append({"d": d, "m": m, "n": n, "batch": batch, "forms": res,
                     "rel_err_split_vs_plain": err})
         del A, X, Y, Yr, pA, pX, pY, pYr
+    # the same five shapes mixed in one call (kmx_kronmult_vmixed), against one
+    # vbatched call per shape over the same instances
+    classes = [(m, n) for m, n, _ in cases]
+    count = 40000
+    rng = np.random.default_rng(SEED)
+    cls = rng.integers(0, len(classes), count).astype(np.int32)
+    fl = 0.0
+    aoff, a_first, xoff, yoff = [], [], [], []
+    na = nx = ny = 0
+    for i in range(count):
+        m, n = classes[cls[i]]
+        a_first.append(len(aoff))
+        for l in range(len(m)):
+            aoff.append(na)
+            na += m[l] * n[l]
+        xoff.append(nx)
+        yoff.append(ny)
+        nx += int(np.prod(n))
+        ny += int(np.prod(m))
+    for c, (m, n) in enumerate(classes):
+        fl += float((cls == c).sum()) * kmx.kron_flops(len(m), m, n)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    A = torch.randn(na, dtype=torch.float64, device="cuda", generator=g) / 3.0
+    X = torch.randn(nx, dtype=torch.float64, device="cuda", generator=g)
+    Y = torch.zeros(ny, dtype=torch.float64, device="cuda")
+    pA = kmx.pointer_array(A, aoff)
+    pX = kmx.pointer_array(X, xoff)
+    pY = kmx.pointer_array(Y, yoff)
+    a_off = torch.tensor(a_first, dtype=torch.int64, device="cuda")
+    dcls = torch.from_numpy(cls).cuda()
+    per = []
+    for c, (m, n) in enumerate(classes):
+        idx = np.nonzero(cls == c)[0]
+        per.append((len(m), m, n, len(idx),
+                    kmx.pointer_array(A, [aoff[a_first[i] + l] for i in idx for l in range(len(m))]),
+                    kmx.pointer_array(X, [xoff[i] for i in idx]),
+                    kmx.pointer_array(Y, [yoff[i] for i in idx])))
+    one = lambda: kmx.kronmult_vmixed(dcls, pA, a_off, pX, pY, classes)  # noqa: E731
+
+    def separate():
+        for d, m, n, b, qa, qx, qy in per:
+            kmx.kronmult_vbatched(d, m, n, qa, qx, qy, None, 0, b)
+
+    ms_one = _events_time(torch, one, max(3, args.steps // 2), 2)
+    ms_sep = _events_time(torch, separate, max(3, args.steps // 2), 2)
+    Y.zero_()
+    one()
+    Y1 = Y.clone()
+    Y.zero_()
+    separate()
+    torch.cuda.synchronize()
+    mixed = {"instances": count, "classes": len(classes),
+             "one_call": {"gflops": round(fl / (ms_one * 1e-3) / 1e9, 1), "ms": round(ms_one, 3)},
+             "per_shape_calls": {"gflops": round(fl / (ms_sep * 1e-3) / 1e9, 1),
+                                 "ms": round(ms_sep, 3)},
+             "rel_err_one_vs_per_shape": float((Y1 - Y).norm() / Y.norm())}
+    del A, X, Y, Y1, pA, pX, pY, per
     kmx.check_device_status()
     print(json.dumps({"metric": "kronmult GFLOP/s, shapes without a specialised kernel (FP64)",
                       "value": out[0]["forms"]["auto"]["gflops"], "unit": "GFLOP/s",
-                      "workload": "rect", "cases": out, "data": "synthetic"}))
+                      "workload": "rect", "cases": out, "mixed_one_call": mixed,
+                      "data": "synthetic"}))
 
 
 def main():

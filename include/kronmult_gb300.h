@@ -308,6 +308,27 @@ int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarra
                            size_t Wcapacity_bytes, const int* classes, int nclasses,
                            const kmx_options* opt, kmx_stream_t stream);
 
+/* Rectangular shapes mixed in one call (the reference needs one
+ * kronmult{d}_vbatched call per shape, kronmult_vbatched.hpp:19-248).  Class c
+ * (nclasses <= 64) is the HOST record classes[13c .. 13c+12] =
+ * (d, m_1..m_6, n_1..n_6), entries past d ignored: factor l is m_l x n_l with
+ * leading dimension m_l, as in vbatched.  Instance i belongs to class cls[i]
+ * (device array); its factors are Aarray[a_off[i] + l], its blocks pX[i]
+ * (prod n_l elements) and pY[i] (prod m_l), accumulated into with atomics (pY
+ * may repeat).  Instances with a class id outside [0, nclasses) are skipped
+ * and flagged in the device status word.  Grouping, launch order and graph
+ * capture as for kmx_kronmult_mixed_*; W slots of twice the class's largest
+ * intermediate, for classes whose entries exceed on-chip memory.  Atomic
+ * accumulation only. */
+int kmx_kronmult_vmixed_f64(int count, const int* cls, const double* const* Aarray,
+                            const long long* a_off, double* const* pX, double* const* pY,
+                            double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,
+                            const kmx_options* opt, kmx_stream_t stream);
+int kmx_kronmult_vmixed_f32(int count, const int* cls, const float* const* Aarray,
+                            const long long* a_off, float* const* pX, float* const* pY, float* W,
+                            size_t Wcapacity_bytes, const int* classes, int nclasses,
+                            const kmx_options* opt, kmx_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Library state and diagnostics.                                          */
 /* ---------------------------------------------------------------------- */

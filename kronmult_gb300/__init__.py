@@ -22,7 +22,7 @@ from ._lib import KmxError, check, exported_symbols, lib, options  # noqa: F401
 __all__ = [
     "KmxError", "lib", "options", "kron_flops", "pointer_array", "check_device_status",
     "kronmult_batched", "kronmult_pbatched", "kronmult_xbatched", "kronmult_vbatched",
-    "set_default_form", "kronmult_mixed", "kronmult_xbatched_wide",
+    "set_default_form", "kronmult_mixed", "kronmult_vmixed", "kronmult_xbatched_wide",
 ]
 
 
@@ -267,6 +267,31 @@ def kronmult_mixed(dims, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes
     rc = fn(count, _addr(dims), _addr(Aarray), _addr(a_off), _addr(pX), _addr(pY), _addr(W), cap,
             cl, len(classes), _opt(form if f64 else None, None, transpose, engine), s)
     check(rc, "kmx_kronmult_mixed")
+
+
+def kronmult_vmixed(cls, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes=None, *,
+                    dtype=None, form=None, transpose=False, engine=None, stream=None):
+    """Instances of mixed rectangular shapes in one call.  cls: int32 CUDA tensor
+    of class ids; classes: host list of (m, n) pairs of per-mode sizes (factor l
+    is m[l] x n[l], leading dimension m[l]); Aarray: factor addresses,
+    instance i's at a_off[i] .. a_off[i]+d-1; pX/pY: block addresses."""
+    t = _torch()
+    f64 = _is_f64(dtype if dtype is not None else t.float64)
+    count = int(cls.numel())
+    flat = []
+    for m, n in classes:
+        d = len(m)
+        if len(n) != d or not 1 <= d <= 6:
+            raise KmxError(1, "kmx_kronmult_vmixed")
+        flat += [d] + [int(v) for v in m] + [1] * (6 - d) + [int(v) for v in n] + [1] * (6 - d)
+    cl = (C.c_int * max(1, len(flat)))(*flat)
+    cap = Wcapacity_bytes if Wcapacity_bytes is not None else (
+        W.numel() * W.element_size() if W is not None else 0)
+    s = C.c_void_p(_stream(stream))
+    fn = lib().kmx_kronmult_vmixed_f64 if f64 else lib().kmx_kronmult_vmixed_f32
+    rc = fn(count, _addr(cls), _addr(Aarray), _addr(a_off), _addr(pX), _addr(pY), _addr(W), cap,
+            cl, len(classes), _opt(form if f64 else None, None, transpose, engine), s)
+    check(rc, "kmx_kronmult_vmixed")
 
 
 # Reference names, one per d, reference argument order.

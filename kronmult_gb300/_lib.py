@@ -95,6 +95,8 @@ _SIGS = {
     "kmx_kgemm_nt_batched_f32": [_i, _i, _i, C.c_float, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp,
                                  _i, _vp],
     "kmx_kronmult_mixed_f32": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
+    "kmx_kronmult_vmixed_f64": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
+    "kmx_kronmult_vmixed_f32": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],
     "kmx_set_default_options": [_optp],
     "kmx_get_default_options": [_optp],
 }

@@ -358,26 +358,22 @@ static int xbatched_impl(int d, int n, const T* const* Aarray, int lda, T* const
   return run_problem(p, sizeof(T) == 8, o, s);
 }
 
-template <typename T>
-static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarray, T* const* pX,
-                         T* const* pY, T* W, size_t Wcap, int batch, const kmx_options* opt,
-                         cudaStream_t s) {
-  if (d < 1 || d > MAXD || batch < 0 || !m || !n) return KMX_ERR_INVALID_ARG;
+// Rectangular shape of one call or class: applied operator A_l (m_l x n_l),
+// or A_l^T (n_l x m_l) when transposed, stored with ld = m_l (the reference's
+// vbatched convention, kronmult_vbatched.hpp:206-211).
+static int rect_problem(Problem& p, int layout, int d, const int* m, const int* n,
+                        const kmx_options& o) {
+  if (d < 1 || d > MAXD || !m || !n) return KMX_ERR_INVALID_ARG;
   for (int l = 0; l < d; ++l)
     if (m[l] < 1 || n[l] < 1) return KMX_ERR_INVALID_ARG;
-  if (batch == 0) return KMX_OK;
-  if (!Aarray || !pX || !pY) return KMX_ERR_NULL_POINTER;
-  kmx_options o = resolve_options(opt);
-  Problem p;
   std::memset(&p, 0, sizeof(p));
-  p.layout = L_VBATCHED;
+  p.layout = layout;
   p.d = d;
-  // applied operator: A_l (m x n), or A_l^T (n x m) when transposed
   for (int l = 0; l < MAXD; ++l) {
     const int ml = (l < d) ? m[l] : 1, nl = (l < d) ? n[l] : 1;
     p.m[l] = o.transpose ? nl : ml;
     p.n[l] = o.transpose ? ml : nl;
-    p.ld[l] = ml;  // the reference's vbatched uses ld = m (kronmult_vbatched.hpp:206-211)
+    p.ld[l] = ml;
   }
   long long Nx = 1, Ny = 1, sxw = 0;
   for (int l = 0; l < d; ++l) {
@@ -396,10 +392,6 @@ static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarr
   p.Nx = Nx;
   p.Ny = Ny;
   p.sxw = sxw;
-  p.count = batch;
-  p.A = Aarray;
-  p.X = pX;
-  p.Y = const_cast<T**>(pY);
   p.trans = o.transpose;
   bool square = true;
   for (int l = 0; l < d; ++l) square = square && (p.m[l] == p.n[0] && p.n[l] == p.n[0]);
@@ -407,13 +399,39 @@ static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarr
     for (int l = 0; l < d; ++l)
       if (p.m[l] == p.n[l] && p.n[l] > GEN_MAXN) return KMX_ERR_UNSUPPORTED;
   }
+  return KMX_OK;
+}
+
+// The caller's workspace W (Wcap bytes) as slots of two sxw buffers.
+template <typename T>
+static void rect_workspace(Problem& p, T* W, size_t Wcap, int count) {
   if (W && Wcap > 0) {
-    const size_t slot_bytes = 2 * (size_t)sxw * sizeof(T);
+    const size_t slot_bytes = 2 * (size_t)p.sxw * sizeof(T);
     p.wmode = 3;
     p.Wbase = W;
-    p.w_stride = 2 * sxw;
-    p.nslots = (int)((Wcap / slot_bytes) < (size_t)batch ? (Wcap / slot_bytes) : (size_t)batch);
+    p.w_stride = 2 * p.sxw;
+    p.nslots = (int)((Wcap / slot_bytes) < (size_t)count ? (Wcap / slot_bytes) : (size_t)count);
   }
+}
+
+template <typename T>
+static int vbatched_impl(int d, const int* m, const int* n, const T* const* Aarray, T* const* pX,
+                         T* const* pY, T* W, size_t Wcap, int batch, const kmx_options* opt,
+                         cudaStream_t s) {
+  if (d < 1 || d > MAXD || batch < 0 || !m || !n) return KMX_ERR_INVALID_ARG;
+  for (int l = 0; l < d; ++l)
+    if (m[l] < 1 || n[l] < 1) return KMX_ERR_INVALID_ARG;
+  if (batch == 0) return KMX_OK;
+  if (!Aarray || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  kmx_options o = resolve_options(opt);
+  Problem p;
+  int rc = rect_problem(p, L_VBATCHED, d, m, n, o);
+  if (rc != KMX_OK) return rc;
+  p.count = batch;
+  p.A = Aarray;
+  p.X = pX;
+  p.Y = const_cast<T**>(pY);
+  rect_workspace(p, W, Wcap, batch);
   return run_problem(p, sizeof(T) == 8, o, s);
 }
 
@@ -466,7 +484,7 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
   rc = cached_workspace(1, need, s, &ws);
   if (rc != KMX_OK) return rc;
   MixedArrays ma;
-  cudaError_t e = mixed_prepare(count, dims, classes, nclasses, ws, need, status, s, &ma);
+  cudaError_t e = mixed_prepare(count, dims, nullptr, classes, nclasses, ws, need, status, s, &ma);
   if (e != cudaSuccess) return cuda_fail(e);
   for (int c = 0; c < nclasses; ++c) {
     const int d = classes[2 * c], n = classes[2 * c + 1];
@@ -492,6 +510,55 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
       const size_t slots = Wcap / slot_bytes;
       p.nslots = (int)(slots < (size_t)count ? slots : (size_t)count);
     }
+    rc = run_problem(p, sizeof(T) == 8, o, s);
+    if (rc != KMX_OK) return rc;
+  }
+  return KMX_OK;
+}
+
+// One call over instances of mixed rectangular shapes: instance i belongs to
+// class cls[i]; class c is the host record classes[13c..13c+12] =
+// (d, m_1..m_6, n_1..n_6).  Grouped on the device like mixed_impl, then one
+// launch per class.
+template <typename T>
+static int vmixed_impl(int count, const int* cls, const T* const* Aarray, const long long* a_off,
+                       T* const* pX, T* const* pY, T* W, size_t Wcap, const int* classes,
+                       int nclasses, const kmx_options* opt, cudaStream_t s) {
+  if (count < 0 || nclasses < 1 || nclasses > KMX_MAX_CLASSES || !classes)
+    return KMX_ERR_INVALID_ARG;
+  kmx_options o = resolve_options(opt);
+  for (int c = 0; c < nclasses; ++c) {
+    Problem p;
+    const int* r = classes + 13 * c;
+    const int rc = rect_problem(p, L_MIXED, r[0], r + 1, r + 7, o);
+    if (rc != KMX_OK) return rc;
+  }
+  if (count == 0) return KMX_OK;
+  if (!cls || !Aarray || !a_off || !pX || !pY) return KMX_ERR_NULL_POINTER;
+  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  int* status = nullptr;
+  int rc = status_ptr(&status);
+  if (rc != KMX_OK) return rc;
+  void* ws = nullptr;
+  const size_t need = mixed_workspace_bytes(count);
+  rc = cached_workspace(1, need, s, &ws);
+  if (rc != KMX_OK) return rc;
+  MixedArrays ma;
+  cudaError_t e = mixed_prepare(count, nullptr, cls, nullptr, nclasses, ws, need, status, s, &ma);
+  if (e != cudaSuccess) return cuda_fail(e);
+  for (int c = 0; c < nclasses; ++c) {
+    const int* r = classes + 13 * c;
+    Problem p;
+    rect_problem(p, L_MIXED, r[0], r + 1, r + 7, o);
+    p.count = count;  // upper bound for the grid; the kernels read the class count
+    p.count_dev = ma.counts + c;
+    p.order = ma.order;
+    p.order_base = ma.offsets + c;
+    p.a_off = a_off;
+    p.A = Aarray;
+    p.X = pX;
+    p.Y = const_cast<T**>(pY);
+    rect_workspace(p, W, Wcap, count);
     rc = run_problem(p, sizeof(T) == 8, o, s);
     if (rc != KMX_OK) return rc;
   }
@@ -614,6 +681,22 @@ int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarra
                            const kmx_options* opt, kmx_stream_t stream) {
   return mixed_impl<float>(count, dims, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
                            nclasses, opt, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_vmixed_f64(int count, const int* cls, const double* const* Aarray,
+                            const long long* a_off, double* const* pX, double* const* pY,
+                            double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,
+                            const kmx_options* opt, kmx_stream_t stream) {
+  return vmixed_impl<double>(count, cls, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
+                             nclasses, opt, KMX_STREAM(stream));
+}
+
+int kmx_kronmult_vmixed_f32(int count, const int* cls, const float* const* Aarray,
+                            const long long* a_off, float* const* pX, float* const* pY, float* W,
+                            size_t Wcapacity_bytes, const int* classes, int nclasses,
+                            const kmx_options* opt, kmx_stream_t stream) {
+  return vmixed_impl<float>(count, cls, Aarray, a_off, pX, pY, W, Wcapacity_bytes, classes,
+                            nclasses, opt, KMX_STREAM(stream));
 }
 
 int kmx_kronmult_xbatched_wide(int in_type, int d, int n, const void* const* Aarray, int lda,

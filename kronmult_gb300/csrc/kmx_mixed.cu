@@ -11,7 +11,8 @@
 //      device memory, so no host synchronisation happens and the whole call
 //      can be captured in a CUDA graph.
 // Instances whose shape is not in the class list are reported through the
-// device status word (DF_BAD_SHAPE) and skipped.
+// device status word (DF_BAD_SHAPE) and skipped.  The rectangular form
+// (kmx_kronmult_vmixed_*) names each instance's class directly.
 #include <cuda_runtime.h>
 
 #include <cub/cub.cuh>
@@ -31,16 +32,21 @@ struct ClassList {
   int count;
 };
 
-__global__ void class_key_kernel(const int* dims, int count, ClassList cl, int* keys, int* ids,
-                                 int* status) {
+__global__ void class_key_kernel(const int* dims, const int* cls, int count, ClassList cl,
+                                 int* keys, int* ids, int* status) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const int d = dims[2 * i], n = dims[2 * i + 1];
     int k = cl.count;
-    for (int c = 0; c < cl.count; ++c)
-      if (cl.d[c] == d && cl.n[c] == n) {
-        k = c;
-        break;
-      }
+    if (cls != nullptr) {
+      const int c = cls[i];
+      if (c >= 0 && c < cl.count) k = c;
+    } else {
+      const int d = dims[2 * i], n = dims[2 * i + 1];
+      for (int c = 0; c < cl.count; ++c)
+        if (cl.d[c] == d && cl.n[c] == n) {
+          k = c;
+          break;
+        }
+    }
     if (k == cl.count) atomicOr(status, DF_BAD_SHAPE);
     keys[i] = k;
     ids[i] = i;
@@ -101,8 +107,9 @@ MixLayout mix_layout(int count) {
 
 size_t mixed_workspace_bytes(int count) { return mix_layout(count).total; }
 
-cudaError_t mixed_prepare(int count, const int* dims, const int* classes, int nclasses, void* ws,
-                          size_t ws_bytes, int* status, cudaStream_t s, MixedArrays* out) {
+cudaError_t mixed_prepare(int count, const int* dims, const int* cls, const int* classes,
+                          int nclasses, void* ws, size_t ws_bytes, int* status, cudaStream_t s,
+                          MixedArrays* out) {
   const MixLayout L = mix_layout(count);
   if (ws == nullptr || ws_bytes < L.total) return cudaErrorInvalidValue;
   if (nclasses < 1 || nclasses > KMX_MAX_CLASSES) return cudaErrorInvalidValue;
@@ -116,14 +123,14 @@ cudaError_t mixed_prepare(int count, const int* dims, const int* classes, int nc
   ClassList cl;
   cl.count = nclasses;
   for (int c = 0; c < nclasses; ++c) {
-    cl.d[c] = classes[2 * c];
-    cl.n[c] = classes[2 * c + 1];
+    cl.d[c] = cls ? 0 : classes[2 * c];
+    cl.n[c] = cls ? 0 : classes[2 * c + 1];
   }
   const int threads = 256;
   int blocks = (count + threads - 1) / threads;
   if (blocks > 4096) blocks = 4096;
   if (blocks < 1) blocks = 1;
-  class_key_kernel<<<blocks, threads, 0, s>>>(dims, count, cl, keys, ids, status);
+  class_key_kernel<<<blocks, threads, 0, s>>>(dims, cls, count, cl, keys, ids, status);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   int bits = 1;

@@ -15,9 +15,11 @@ struct MixedArrays {
 
 size_t mixed_workspace_bytes(int count);
 
-// classes: host array of nclasses (d, n) pairs; dims: device array of
-// count (d, n) pairs.
-cudaError_t mixed_prepare(int count, const int* dims, const int* classes, int nclasses, void* ws,
-                          size_t ws_bytes, int* status, cudaStream_t s, MixedArrays* out);
+// Either dims (device array of count (d, n) pairs, matched against classes,
+// a host array of nclasses (d, n) pairs) or cls (device array of count class
+// ids below nclasses; classes unused) gives each instance its class.
+cudaError_t mixed_prepare(int count, const int* dims, const int* cls, const int* classes,
+                          int nclasses, void* ws, size_t ws_bytes, int* status, cudaStream_t s,
+                          MixedArrays* out);
 
 }  // namespace kmx

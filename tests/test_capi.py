@@ -145,3 +145,18 @@ def test_xbatched_build_argument_checks_without_gpu(kmx):
         empty[1] = 0
         assert fn(*empty) == 0
     assert L.kmx_xbatched_build_workspace_bytes(1000) >= 4 * 4 * 1000
+
+
+def test_vmixed_argument_checks_without_gpu(kmx):
+    L = kmx.lib()
+    good = (C.c_int * 13)(2, 3, 4, 1, 1, 1, 1, 4, 5, 1, 1, 1, 1)
+    bad_d = (C.c_int * 13)(7, 3, 4, 1, 1, 1, 1, 4, 5, 1, 1, 1, 1)
+    bad_m = (C.c_int * 13)(2, 3, 0, 1, 1, 1, 1, 4, 5, 1, 1, 1, 1)
+    for fn in (L.kmx_kronmult_vmixed_f64, L.kmx_kronmult_vmixed_f32):
+        assert fn(4, 8, 8, 8, 8, 8, 0, 0, good, 0, None, None) == 1   # no classes
+        assert fn(4, 8, 8, 8, 8, 8, 0, 0, good, 65, None, None) == 1  # too many classes
+        assert fn(4, 8, 8, 8, 8, 8, 0, 0, bad_d, 1, None, None) == 1  # d outside 1..6
+        assert fn(4, 8, 8, 8, 8, 8, 0, 0, bad_m, 1, None, None) == 1  # a zero extent
+        assert fn(-1, 8, 8, 8, 8, 8, 0, 0, good, 1, None, None) == 1  # negative count
+        assert fn(4, 0, 8, 8, 8, 8, 0, 0, good, 1, None, None) == 2   # no class ids
+        assert fn(0, 0, 0, 0, 0, 0, 0, 0, good, 1, None, None) == 0   # empty call
