@@ -135,3 +135,88 @@ def test_fullsize_sampled_blocks_vs_oracle(kmx, oracle, wl):
     num = np.linalg.norm(got - Yref, axis=1)
     den = np.maximum(np.linalg.norm(Yref, axis=1), 1e-300)
     assert float((num / den).max()) <= F64_TOL
+
+
+# ---------------------------------------------------------------------------
+# the precision-form workload at full size: xbatched d=4 n=8 and d=3 n=16,
+# 262144 entries over 16384 X/Y blocks, factors N(0,1)/sqrt(n), X N(0,1)
+# ---------------------------------------------------------------------------
+
+F32_FORM_TOL = 1e-6   # FP32-stored forms, against FP64 on the unrounded inputs
+BF16_FORM_TOL = 1e-2  # BF16 storage: the error of rounding inputs to 8 bits
+
+
+def _precision_case(d, n, seed):
+    entries, nblocks, pool = 262144, 16384, 1024
+    N = n ** d
+    rng = np.random.default_rng(seed)
+    counts = rng.geometric(1.0 / 16, nblocks)
+    y_idx = np.repeat(np.arange(nblocks), counts)[:entries]
+    if len(y_idx) < entries:
+        y_idx = np.concatenate([y_idx, rng.integers(0, nblocks, entries - len(y_idx))])
+    rng.shuffle(y_idx)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    A = torch.randn((d, pool, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
+    X = torch.randn((nblocks, N), dtype=torch.float64, device="cuda", generator=g)
+    return dict(d=d, n=n, N=N, pool=pool, entries=entries, A=A, X=X,
+                ai=torch.from_numpy(rng.integers(0, pool, (entries, d))).cuda(),
+                xi=torch.from_numpy(rng.integers(0, nblocks, entries)).cuda(),
+                yi=torch.from_numpy(y_idx).cuda())
+
+
+def _pc_ptrs(c, A, X, Y):
+    lvl = torch.arange(c["d"], device="cuda")[None, :]
+    n, N = c["n"], c["N"]
+    return (((lvl * c["pool"] + c["ai"]) * (n * n * A.element_size()) + A.data_ptr())
+            .reshape(-1).contiguous(),
+            c["xi"] * (N * X.element_size()) + X.data_ptr(),
+            c["yi"] * (N * Y.element_size()) + Y.data_ptr())
+
+
+def _scaled_blockwise(y, yref):
+    s = yref.abs().amax(dim=1, keepdim=True).clamp_min(1e-300)
+    return float((torch.linalg.vector_norm((y - yref) / s, dim=1) /
+                  torch.linalg.vector_norm(yref / s, dim=1).clamp_min(1e-300)).max())
+
+
+@pytest.mark.parametrize("d,n", [(4, 8), (3, 16)])
+def test_fullsize_precision_forms(kmx, d, n):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    c = _precision_case(d, n, 31 + n)
+    Yref = torch.zeros_like(c["X"])
+    pA, pX, pY = _pc_ptrs(c, c["A"], c["X"], Yref)
+    kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, c["entries"], form="plain")
+    Y = torch.zeros_like(Yref)
+    pA, pX, pY = _pc_ptrs(c, c["A"], c["X"], Y)
+    kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, c["entries"])
+    torch.cuda.synchronize()
+    assert _blockwise(Y, Yref) <= F64_TOL
+    for tdt, tol in ((torch.float32, F32_FORM_TOL), (torch.bfloat16, BF16_FORM_TOL)):
+        A, X = c["A"].to(tdt), c["X"].to(tdt)
+        ind = "f32" if tdt == torch.float32 else "bf16"
+        for form, acc in ((None, None), ("tf32x3", None), ("tf32x3", "deterministic")):
+            Y.zero_()
+            pA, pX, pY = _pc_ptrs(c, A, X, Y)
+            kmx.kronmult_xbatched_wide(d, n, pA, n, pX, pY, c["entries"], in_dtype=ind,
+                                       form=form, accumulate=acc)
+            torch.cuda.synchronize()
+            assert _scaled_blockwise(Y, Yref) <= tol, (ind, form, acc)
+            if acc == "deterministic":
+                Y2 = torch.zeros_like(Y)
+                kmx.kronmult_xbatched_wide(d, n, pA, n, pX, c["yi"] * (c["N"] * 8) + Y2.data_ptr(),
+                                           c["entries"], in_dtype=ind, form=form, accumulate=acc)
+                torch.cuda.synchronize()
+                assert torch.equal(Y, Y2)
+        del A, X
+    # the FP32 entry point proper (FP32 X, factors and Y)
+    A32, X32 = c["A"].float(), c["X"].float()
+    Y32 = torch.zeros(c["X"].shape, dtype=torch.float32, device="cuda")
+    pA, pX, pY = _pc_ptrs(c, A32, X32, Y32)
+    for form in (None, "tf32x3"):
+        Y32.zero_()
+        kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, c["entries"], dtype=torch.float32,
+                              form=form)
+        torch.cuda.synchronize()
+        assert _scaled_blockwise(Y32.double(), Yref) <= F32_FORM_TOL, form
+    assert kmx.check_device_status() == 0
