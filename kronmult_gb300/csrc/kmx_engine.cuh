@@ -466,9 +466,15 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) 
 // Split (double-float) form, square factors, compile-time NN.  Same data flow
 // as the plain form; the shared intermediate holds (hi, lo) pairs.  An entry
 // whose inputs hold Inf/NaN is evaluated by the plain FP64 code instead.
+// With the intermediate in the global workspace (GBUF: entries of 16K+
+// elements, groups of 512 threads) the kernel waits on L2 and needs two CTAs
+// per SM, so for n <= 8 it is held to 64 registers (measured on GB300, d=6
+// n=8: 2321 GFLOP/s at 64 registers against 1963 at the 116 the compiler
+// otherwise takes); a minimum of 0 CTAs leaves the on-chip variants' register
+// choice to the compiler.
 // ---------------------------------------------------------------------------
 template <int NN, bool GBUF>
-__global__ void __launch_bounds__(MAX_THREADS) sq_split_kernel(const Problem p) {
+__global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_split_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int G = p.group_threads;
   const int E = p.groups_per_cta;

@@ -127,3 +127,43 @@ def test_autograd_backward_matches_fused(kmx):
     assert blockwise_rel_err(X.grad.cpu().numpy(), dX.cpu().numpy()) <= 1e-14
     assert blockwise_rel_err(A.grad.reshape(5, -1).cpu().numpy(),
                              dA.reshape(5, -1).cpu().numpy()) <= 1e-14
+
+
+@pytest.mark.parametrize("d,n,batch", [(6, 5, 1024), (3, 8, 4096)])
+def test_fused_grad_fullsize_identities(kmx, d, n, batch):
+    """At the benchmark sizes, exact identities instead of differences:
+    Y equals the forward, dX equals the transposed forward of G, and for each
+    mode k, K is linear in A_k, so sum(G * K(A with A_k := E) X) = <dA_k, E>
+    entry by entry."""
+    from kronmult_gb300.autograd import kronmult_fused_grad
+
+    g = torch.Generator(device="cuda").manual_seed(40 + d)
+    A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
+    X = torch.randn((batch, n ** d), dtype=torch.float64, device="cuda", generator=g)
+    G = torch.randn((batch, n ** d), dtype=torch.float64, device="cuda", generator=g)
+    Y, dX, dA = kronmult_fused_grad(A, X, G)
+    torch.cuda.synchronize()
+    Yf = torch.zeros_like(X)
+    kmx.kronmult_batched(d, n, A, X, Yf, None, batch, form="plain")
+    dXf = torch.zeros_like(X)
+    kmx.kronmult_batched(d, n, A, G, dXf, None, batch, form="plain", transpose=True)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float((torch.linalg.vector_norm(a - b, dim=1) /
+                      torch.linalg.vector_norm(b, dim=1).clamp_min(1e-300)).max())
+
+    assert rel(Y, Yf) <= 1e-13
+    assert rel(dX, dXf) <= 1e-13
+    E = torch.randn((batch, n, n), dtype=torch.float64, device="cuda", generator=g)
+    for k in range(d):
+        Ak = A.clone()
+        Ak[:, k] = E
+        Z = torch.zeros_like(X)
+        kmx.kronmult_batched(d, n, Ak, X, Z, None, batch, form="plain")
+        torch.cuda.synchronize()
+        lhs = (G * Z).sum(dim=1)
+        rhs = (dA[:, k] * E).sum(dim=(1, 2))
+        scale = torch.linalg.vector_norm(G, dim=1) * torch.linalg.vector_norm(Z, dim=1)
+        assert float(((lhs - rhs).abs() / scale).max()) <= 1e-13, k
+    assert kmx.check_device_status() == 0
