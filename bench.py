@@ -87,18 +87,22 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per entry of the split kernel from the committed ncu summary
-    (profiles/), or None."""
-    p = os.path.join(ROOT, "profiles", "xbatched_d6n4_traffic.txt")
+def profile_value(name, key):
+    """A `key = value` line of a committed ncu summary (profiles/), or None."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_entry"):
+                if line.startswith(key):
                     return float(line.split("=")[1].split()[0])
-    except OSError:
+    except (OSError, ValueError, IndexError):
         pass
     return None
+
+
+def profile_traffic():
+    """DRAM bytes per entry of the split kernel from the committed ncu summary."""
+    return profile_value("xbatched_d6n4_traffic.txt", "dram_bytes_per_entry")
 
 
 class ClockSampler:
@@ -464,6 +468,22 @@ def run_ours(args):
              "frac_chosen": round(max(t_fp64, t_hbm) / (ms * 1e-3), 3),
              "frac_plain": round(max(t_fp64, t_hbm) / (ms_plain * 1e-3), 3)}
 
+    # the binding resource of the chosen form: FP32 instruction issue.  Warp-
+    # instructions per entry from the committed ncu summary of the kernel;
+    # peak = 4 schedulers x SMs x the SM clock sampled in the timed region.
+    issue = None
+    ipe = profile_value("xbatched_d6n4_split_tile_kernel.md", "warp_instructions_per_entry")
+    sm_mhz = (clocks or {}).get("sm_mhz")
+    if ipe and sm_mhz:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        ach = ipe * entries / (ms * 1e-3)
+        peak = 4.0 * sms * sm_mhz * 1e6
+        issue = {"bound": "fp32 issue", "unit": "warp-instructions/s",
+                 "instructions_per_entry": ipe, "achieved": float(f"{ach:.4g}"),
+                 "peak": float(f"{peak:.4g}"), "frac": round(ach / peak, 3),
+                 "source": "ncu smsp__inst_executed.sum of the kernel "
+                           "(profiles/xbatched_d6n4_split_tile_kernel.md)"}
+
     cpu = None if args.no_cpu_baseline else cpu_baseline(w)
     line = {
         "metric": METRIC,
@@ -485,7 +505,7 @@ def run_ours(args):
                    "note": "FP64 as base-2^9 digits, exact FP16 tensor-core products "
                            "(mma.sync), double-float pass for handed-back entries"},
         "rel_err_chosen_vs_plain": err_vs_plain,
-        "roofline": roofline, "fp64_roofline": north,
+        "roofline": roofline, "fp64_roofline": north, "issue_roofline": issue,
         "gpu_launches": args.steps, "gpu_launches_deterministic_per_step": 8, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
