@@ -276,10 +276,18 @@ int kmx_kgemm_nt_batched_f32(int mm, int nn, int kk, float alpha, float* const* 
  * otherwise slots for the concurrently processed entries. */
 size_t kmx_grad_workspace_bytes(int d, int n, int batchCount, int fp64);
 
+/* FP64 arithmetic form: the library default (kmx_set_default_options), whose
+ * AUTO runs the mode products and Gram sums in double-float on the FP32 pipe
+ * (entries holding Inf/NaN or an all-zero X, G or factor in FP64); _ex takes
+ * it from opt->form (KMX_FORM_PLAIN: native FP64).  FP32 data: FP32 FMA. */
 int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
                                   const double* G, double* Y, double* dX, double* dA,
                                   double* W, size_t Wcapacity_bytes, int batchCount,
                                   kmx_stream_t stream);
+int kmx_kronmult_batched_grad_f64_ex(int d, int n, const double* A, const double* X,
+                                     const double* G, double* Y, double* dX, double* dA,
+                                     double* W, size_t Wcapacity_bytes, int batchCount,
+                                     const kmx_options* opt, kmx_stream_t stream);
 int kmx_kronmult_batched_grad_f32(int d, int n, const float* A, const float* X, const float* G,
                                   float* Y, float* dX, float* dA, float* W,
                                   size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream);

@@ -77,6 +77,8 @@ _SIGS = {
     "kmx_release_workspace": [_vp],
     "kmx_kronmult_xbatched_f64_noalloc": [_i, _i, _vp, _i, _vp, _vp, _i, _vp],
     "kmx_kronmult_batched_grad_f64": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp],
+    "kmx_kronmult_batched_grad_f64_ex": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i,
+                                         _optp, _vp],
     "kmx_kronmult_batched_grad_f32": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp],
     "kmx_kronmult_xbatched_wide": [_i, _i, _i, _vp, _i, _vp, _vp, _i, _optp, _vp],
     "kmx_kronmult_mixed_f64": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _ip, _i, _optp, _vp],

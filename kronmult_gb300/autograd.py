@@ -7,7 +7,8 @@ Layout (the reference's batched layout, kronmult6_batched.hpp:14-94):
 
 Forward runs the tuned forward kernel; backward runs the fused kernel that
 recomputes the forward intermediates on chip (nothing is stored between the
-two) and returns dA, dX.
+two) and returns dA, dX -- in double-float for FP64 data unless the forward
+asked for form="plain".
 """
 from __future__ import annotations
 
@@ -18,17 +19,22 @@ import torch
 from . import _lib, kronmult_batched
 
 
-def _grad_call(d, n, A, X, G, Y, dX, dA, W):
+def _grad_call(d, n, A, X, G, Y, dX, dA, W, form=None):
     L = _lib.lib()
     f64 = A.dtype == torch.float64
-    fn = L.kmx_kronmult_batched_grad_f64 if f64 else L.kmx_kronmult_batched_grad_f32
 
     def a(t):
         return t.data_ptr() if t is not None else None
 
     cap = W.numel() * W.element_size() if W is not None else 0
-    rc = fn(d, n, a(A), a(X), a(G), a(Y), a(dX), a(dA), a(W), cap, A.shape[0],
-            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if f64:
+        opt = None if form is None else C.byref(_lib.options(form))
+        rc = L.kmx_kronmult_batched_grad_f64_ex(d, n, a(A), a(X), a(G), a(Y), a(dX), a(dA), a(W),
+                                                cap, A.shape[0], opt, s)
+    else:
+        rc = L.kmx_kronmult_batched_grad_f32(d, n, a(A), a(X), a(G), a(Y), a(dX), a(dA), a(W),
+                                             cap, A.shape[0], s)
     _lib.check(rc, "kmx_kronmult_batched_grad")
 
 
@@ -43,14 +49,15 @@ def grad_workspace(d, n, batch, dtype=torch.float64, device="cuda"):
     return torch.empty((nbytes + esz - 1) // esz, dtype=dtype, device=device)
 
 
-def kronmult_fused_grad(A, X, G, want_y=True):
-    """Y, dX, dA of loss = sum(G * Y) in one launch."""
+def kronmult_fused_grad(A, X, G, want_y=True, form=None):
+    """Y, dX, dA of loss = sum(G * Y) in one launch.  form: None (the library
+    default: double-float for FP64), "split", or "plain" (native FP64)."""
     batch, d, n, _ = A.shape
     Y = torch.zeros_like(X) if want_y else None
     dX = torch.zeros_like(X)
     dA = torch.zeros_like(A)
     _grad_call(d, n, A.contiguous(), X.contiguous(), G.contiguous(), Y, dX, dA,
-               grad_workspace(d, n, batch, A.dtype))
+               grad_workspace(d, n, batch, A.dtype), form)
     return Y, dX, dA
 
 
@@ -63,6 +70,7 @@ class KronmultFunction(torch.autograd.Function):
         Y = torch.zeros_like(X)
         kronmult_batched(d, n, A, X, Y, None, batch, form=form)
         ctx.save_for_backward(A, X)
+        ctx.form = form
         return Y
 
     @staticmethod
@@ -72,7 +80,10 @@ class KronmultFunction(torch.autograd.Function):
         need_a, need_x = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         dX = torch.zeros_like(X) if need_x else None
         dA = torch.zeros_like(A) if need_a else None
-        _grad_call(d, n, A, X, G.contiguous(), None, dX, dA, grad_workspace(d, n, batch, A.dtype))
+        # the backward follows the forward's arithmetic form ("plain": FP64)
+        form = "plain" if ctx.form == "plain" else None
+        _grad_call(d, n, A, X, G.contiguous(), None, dX, dA, grad_workspace(d, n, batch, A.dtype),
+                   form)
         return dA, dX, None
 
 

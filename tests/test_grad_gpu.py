@@ -43,8 +43,12 @@ def explicit_grads(A, X, G):
     return dX, dA
 
 
-@pytest.mark.parametrize("d,n", [(1, 3), (2, 4), (3, 3), (4, 2), (3, 5)])
-def test_fused_grad_vs_explicit_kron(kmx, d, n):
+GRAD_FORMS = ["split", "plain"]  # double-float (the default for FP64) and native FP64
+
+
+@pytest.mark.parametrize("form", GRAD_FORMS)
+@pytest.mark.parametrize("d,n", [(1, 3), (2, 4), (3, 3), (4, 2), (3, 5), (2, 7), (3, 8), (4, 6)])
+def test_fused_grad_vs_explicit_kron(kmx, d, n, form):
     from kronmult_gb300.autograd import kronmult_fused_grad
 
     rng = np.random.default_rng(d * 10 + n)
@@ -52,7 +56,7 @@ def test_fused_grad_vs_explicit_kron(kmx, d, n):
     A = rng.standard_normal((batch, d, n, n))
     X = rng.standard_normal((batch, N))
     G = rng.standard_normal((batch, N))
-    Y, dX, dA = kronmult_fused_grad(*(torch.from_numpy(t).cuda() for t in (A, X, G)))
+    Y, dX, dA = kronmult_fused_grad(*(torch.from_numpy(t).cuda() for t in (A, X, G)), form=form)
     ex_dX, ex_dA = explicit_grads(A, X, G)
     assert blockwise_rel_err(dX.cpu().numpy(), ex_dX) <= 1e-13
     assert blockwise_rel_err(dA.cpu().numpy().reshape(batch, -1), ex_dA.reshape(batch, -1)) <= 1e-13
@@ -60,11 +64,13 @@ def test_fused_grad_vs_explicit_kron(kmx, d, n):
     Y2 = torch.zeros_like(Y)
     kmx.kronmult_batched(d, n, torch.from_numpy(A).cuda(), torch.from_numpy(X).cuda(), Y2, None,
                          batch, form="plain")
-    assert blockwise_rel_err(Y.cpu().numpy(), Y2.cpu().numpy()) <= 1e-14
+    assert blockwise_rel_err(Y.cpu().numpy(), Y2.cpu().numpy()) <= (1e-14 if form == "plain"
+                                                                     else 1e-13)
 
 
+@pytest.mark.parametrize("form", GRAD_FORMS)
 @pytest.mark.parametrize("d,n,batch", [(6, 5, 3), (3, 8, 8), (6, 4, 4)])
-def test_fused_grad_central_differences(kmx, d, n, batch):
+def test_fused_grad_central_differences(kmx, d, n, batch, form):
     """64 random coordinates of X and of each A_i, h = 1e-6: the loss is linear
     in every single coordinate, so central differences are exact up to rounding."""
     from kronmult_gb300.autograd import kronmult_fused_grad
@@ -74,7 +80,7 @@ def test_fused_grad_central_differences(kmx, d, n, batch):
     A = torch.from_numpy(rng.standard_normal((batch, d, n, n)) / np.sqrt(n)).cuda()
     X = torch.from_numpy(rng.standard_normal((batch, N))).cuda()
     G = torch.from_numpy(rng.standard_normal((batch, N))).cuda()
-    _, dX, dA = kronmult_fused_grad(A, X, G, want_y=False)
+    _, dX, dA = kronmult_fused_grad(A, X, G, want_y=False, form=form)
 
     def loss(Av, Xv, b):
         # only entry b depends on the perturbed coordinate
@@ -129,8 +135,9 @@ def test_autograd_backward_matches_fused(kmx):
                              dA.reshape(5, -1).cpu().numpy()) <= 1e-14
 
 
+@pytest.mark.parametrize("form", GRAD_FORMS)
 @pytest.mark.parametrize("d,n,batch", [(6, 5, 1024), (3, 8, 4096)])
-def test_fused_grad_fullsize_identities(kmx, d, n, batch):
+def test_fused_grad_fullsize_identities(kmx, d, n, batch, form):
     """At the benchmark sizes, exact identities instead of differences:
     Y equals the forward, dX equals the transposed forward of G, and for each
     mode k, K is linear in A_k, so sum(G * K(A with A_k := E) X) = <dA_k, E>
@@ -141,7 +148,7 @@ def test_fused_grad_fullsize_identities(kmx, d, n, batch):
     A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
     X = torch.randn((batch, n ** d), dtype=torch.float64, device="cuda", generator=g)
     G = torch.randn((batch, n ** d), dtype=torch.float64, device="cuda", generator=g)
-    Y, dX, dA = kronmult_fused_grad(A, X, G)
+    Y, dX, dA = kronmult_fused_grad(A, X, G, form=form)
     torch.cuda.synchronize()
     Yf = torch.zeros_like(X)
     kmx.kronmult_batched(d, n, A, X, Yf, None, batch, form="plain")
@@ -167,3 +174,33 @@ def test_fused_grad_fullsize_identities(kmx, d, n, batch):
         scale = torch.linalg.vector_norm(G, dim=1) * torch.linalg.vector_norm(Z, dim=1)
         assert float(((lhs - rhs).abs() / scale).max()) <= 1e-13, k
     assert kmx.check_device_status() == 0
+
+
+def test_split_grad_special_entries_run_fp64(kmx):
+    """Entries with Inf/NaN, or an all-zero X, G or factor, are evaluated in FP64
+    by the double-float kernel: NaN/Inf land where FP64 puts them and the zero
+    cases match the FP64 kernel; the other entries stay within tolerance."""
+    from kronmult_gb300.autograd import kronmult_fused_grad
+
+    rng = np.random.default_rng(77)
+    d, n, batch = 4, 5, 6
+    N = n ** d
+    A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+    X = rng.standard_normal((batch, N))
+    G = rng.standard_normal((batch, N))
+    X[1, 7] = np.inf
+    A[2, 1, 0, 3] = np.nan
+    A[3, 2] = 0.0     # zero factor: dA_2 of entry 3 is still nonzero
+    X[4] = 0.0        # zero X: dX of entry 4 is still nonzero
+    G[5] = 0.0
+    T = [torch.from_numpy(t).cuda() for t in (A, X, G)]
+    Ys, dXs, dAs = kronmult_fused_grad(*T, form="split")
+    Yp, dXp, dAp = kronmult_fused_grad(*T, form="plain")
+    for s_, p_ in ((Ys, Yp), (dXs, dXp), (dAs.reshape(batch, -1), dAp.reshape(batch, -1))):
+        s_, p_ = s_.cpu().numpy(), p_.cpu().numpy()
+        assert np.array_equal(np.isnan(s_), np.isnan(p_))
+        assert np.array_equal(np.isinf(s_), np.isinf(p_))
+        for b in (0, 3, 4, 5):
+            assert np.array_equal(s_[b], p_[b]) or blockwise_rel_err(s_[b:b + 1], p_[b:b + 1]) <= 1e-13
+    assert np.array_equal(dAs[3].cpu().numpy(), dAp[3].cpu().numpy())  # FP64 path taken
+    assert np.abs(dAs[3, 2].cpu().numpy()).max() > 0
