@@ -321,7 +321,9 @@ __device__ __forceinline__ void mode_apply_df(const double* X, int ex, const df*
     const long long base = (long long)o * NN * s + r0;
     df v[NN];
     load_fiber<NN, FROM_X>(v, X, ex, src, base, s);
-#pragma unroll
+    // rows one at a time above n = 5: all NN^2 factor pairs in registers at
+    // once would cost the occupancy these small-block launches need
+#pragma unroll(NN <= 5 ? NN : 1)
     for (int a = 0; a < NN; ++a) {
       df ar[NN];
 #pragma unroll
@@ -383,8 +385,17 @@ __device__ __forceinline__ void mode_gram_df(const df* B, const double* X, int e
   }
 }
 
+// The FP64 path for the split kernel's special entries, out of line so that
+// its registers do not set the kernel's.
 template <int NN>
-__global__ void __launch_bounds__(NN <= 5 ? 512 : 256) grad_split_kernel(const GradProblem gp) {
+__device__ __noinline__ void grad_entry_fp64(const GradProblem& gp, long long e, double* sA,
+                                             double* sdA, double* sB, double* sRed, double* Fst,
+                                             int lt, int G) {
+  grad_entry<double, NN>(gp, e, sA, sdA, sB, sRed, Fst, lt, G);
+}
+
+template <int NN>
+__global__ void __launch_bounds__(NN <= 5 ? 512 : 256, NN <= 5 ? 0 : 2) grad_split_kernel(const GradProblem gp) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NN2 = NN * NN;
   const int d = gp.d, N = gp.N, F = N / NN;
@@ -439,7 +450,7 @@ __global__ void __launch_bounds__(NN <= 5 ? 512 : 256) grad_split_kernel(const G
     }
     // (sExp is reset only by the next entry, after this entry's last barrier)
     if (special) {
-      grad_entry<double, NN>(gp, e, m.sA, m.sdA, m.sB, m.sRed, Fst, lt, G);
+      grad_entry_fp64<NN>(gp, e, m.sA, m.sdA, m.sB, m.sRed, Fst, lt, G);
       continue;
     }
     const int sx = ex - 1023, sg = eg - 1023;
