@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(NN <= 5 ? 512 : 256) grad_kernel(const GradPro
 //   F_k: sx + sum_{l<k} sa_l,   B_k: sg + sum_{l>k} sa_l,
 //   dA_k: sg + sx + sum_{l!=k} sa_l,   Y and dX: sx (sg) + sum_l sa_l,
 // and are widened to FP64 by exponent arithmetic where they leave.  The Gram
-// partials of each thread are widened before the (FP64) block reduction.
+// partials of a block are reduced as pairs and widened once per output.
 // Entries with Inf/NaN or an all-zero X, G or factor run grad_entry in FP64
 // (so IEEE propagation and exact zeros are those of FP64).
 // ---------------------------------------------------------------------------
@@ -286,16 +286,70 @@ struct DfSum {
     s = t;
     c = __fadd_rn(c, __fadd_rn(te, e));
   }
+  // the sum as a normalised pair
+  __device__ __forceinline__ df pair() const {
+    df r;
+    r.hi = __fadd_rn(s, c);
+    r.lo = __fsub_rn(c, __fsub_rn(r.hi, s));
+    return r;
+  }
   // the sum times 2^escale, in FP64
   __device__ __forceinline__ double widen(int escale) const {
-    const float hi = __fadd_rn(s, c);
-    const float lo = __fsub_rn(c, __fsub_rn(hi, s));
-    return f32_to_f64_scaled(hi, escale) + f32_to_f64_scaled(lo, escale);
+    const df r = pair();
+    return f32_to_f64_scaled(r.hi, escale) + f32_to_f64_scaled(r.lo, escale);
   }
 };
 
 __device__ __forceinline__ double widen_pair(df v, int escale) {
   return f32_to_f64_scaled(v.hi, escale) + f32_to_f64_scaled(v.lo, escale);
+}
+
+// a + b for normalised pairs (same scale): exact two-sum of the high parts,
+// low parts and error added, renormalised.
+__device__ __forceinline__ df df_add(df a, df b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  df r;
+  r.hi = __fadd_rn(s, e);
+  r.lo = __fsub_rn(e, __fsub_rn(r.hi, s));
+  return r;
+}
+
+// The pair form of gram_reduce: the G threads' partials (all at one scale)
+// are summed as pairs on the FP32 pipe and widened once per output,
+// sdA[q] += 2^escale * sum.  sRed holds pairs in the FP64 slots.  Every
+// thread of the block calls it.
+template <int NN>
+__device__ __forceinline__ void gram_reduce_df(const df (&acc)[NN * NN], double* sdA,
+                                               double* sRed, int escale, int lt, int G) {
+  constexpr int NN2 = NN * NN;
+  df* sR = reinterpret_cast<df*>(sRed);
+  const int GH = G / 2;
+#pragma unroll
+  for (int q = 0; q < NN2; ++q) {
+    df other;
+    other.hi = __shfl_down_sync(0xffffffffu, acc[q].hi, 1);
+    other.lo = __shfl_down_sync(0xffffffffu, acc[q].lo, 1);
+    if ((lt & 1) == 0) sR[q * GH + (lt >> 1)] = df_add(acc[q], other);
+  }
+  __syncthreads();
+  const int nch = GH / 32;
+  df* sR2 = sR + NN2 * GH;
+  for (int t = lt; t < NN2 * nch; t += G) {
+    const int q = t / nch, c = t - q * nch;
+    const df* src = sR + q * GH + c * 32;
+    df v = src[0];
+#pragma unroll 8
+    for (int i = 1; i < 32; ++i) v = df_add(v, src[i]);
+    sR2[t] = v;
+  }
+  __syncthreads();
+  for (int q = lt; q < NN2; q += G) {
+    df v = sR2[q * nch];
+    for (int c = 1; c < nch; ++c) v = df_add(v, sR2[q * nch + c]);
+    sdA[q] += widen_pair(v, escale);
+  }
 }
 
 // One fiber's NN values: FP64 X split on the fly (FROM_X), else stored pairs.
@@ -362,10 +416,10 @@ __device__ __forceinline__ void mode_gram_df(const df* B, const double* X, int e
 #pragma unroll
         for (int b = 0; b < NN; ++b) acc[a * NN + b].add(bv[a], x[b]);
     }
-    double w[NN2];
+    df w[NN2];
 #pragma unroll
-    for (int q = 0; q < NN2; ++q) w[q] = acc[q].widen(escale);
-    gram_reduce<double, NN>(w, sdA, sRed, lt, G);
+    for (int q = 0; q < NN2; ++q) w[q] = acc[q].pair();
+    gram_reduce_df<NN>(w, sdA, sRed, escale, lt, G);
   } else {
     const int chunks = G / NN2;
     if (lt >= chunks * NN2) return;
