@@ -43,9 +43,10 @@ typedef enum kmx_status {
                                 through the device status word, bit 16) */
 } kmx_status;
 
-/* Arithmetic form.  FP64 entry points: AUTO, PLAIN, SPLIT.  FP32-stored
- * entry points (the _f32 functions and kmx_kronmult_xbatched_wide): FP32
- * fused multiply-add unless TF32X3 is asked for. */
+/* Arithmetic form.  FP64 entry points: AUTO, PLAIN, SPLIT, DIGITS (the fused
+ * backward: PLAIN runs FP64, the others double-float).  FP32-stored entry
+ * points (the _f32 functions and kmx_kronmult_xbatched_wide): FP32 fused
+ * multiply-add unless TF32X3 is asked for. */
 typedef enum kmx_form {
   KMX_FORM_AUTO = 0,   /* square shapes: per-(d,n) choice from the tuning table;
                           other shapes: SPLIT once an X or Y block has 512 or more
