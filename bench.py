@@ -886,8 +886,10 @@ def run_rect(args):
         ([10] * 4, [10] * 4, 8192),
         ([12] * 3, [12] * 3, 16384),
     ]
+    # beyond shared memory (25088-element blocks): intermediates in the workspace
+    big = [([8, 7, 8, 7, 8], [7, 8, 7, 8, 8], 2048)]
     out = []
-    for m, n, batch in cases:
+    for m, n, batch in cases + big:
         d = len(m)
         Nx, Ny = int(np.prod(n)), int(np.prod(m))
         g = torch.Generator(device="cuda").manual_seed(SEED + d)
@@ -901,24 +903,28 @@ def run_rect(args):
         pX = kmx.pointer_array(X, np.arange(batch) * Nx)
         pY = kmx.pointer_array(Y, np.arange(batch) * Ny)
         fl = batch * kmx.kron_flops(d, m, n)
+        W = None
+        if (m, n, batch) in big:
+            sxw = max([Nx] + [int(np.prod(m[:k])) * int(np.prod(n[k:])) for k in range(1, d + 1)])
+            W = torch.empty(2 * sxw * 512, dtype=torch.float64, device="cuda")  # 512 slots
         res = {}
         for name in ("split", "plain", "auto"):
-            call = lambda: kmx.kronmult_vbatched(d, m, n, pA, pX, pY, None, 0, batch, form=name)
+            call = lambda: kmx.kronmult_vbatched(d, m, n, pA, pX, pY, W, None, batch, form=name)
             ms = _events_time(torch, call, max(3, args.steps // 2), 2)
             res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3)}
         Yr = torch.zeros_like(Y)
         pYr = kmx.pointer_array(Yr, np.arange(batch) * Ny)
-        kmx.kronmult_vbatched(d, m, n, pA, pX, pYr, None, 0, batch, form="plain")
+        kmx.kronmult_vbatched(d, m, n, pA, pX, pYr, W, None, batch, form="plain")
         Y.zero_()
-        kmx.kronmult_vbatched(d, m, n, pA, pX, pY, None, 0, batch, form="split")
+        kmx.kronmult_vbatched(d, m, n, pA, pX, pY, W, None, batch, form="split")
         torch.cuda.synchronize()
         err = float((torch.linalg.vector_norm(Y - Yr, dim=1) /
                      torch.linalg.vector_norm(Yr, dim=1)).max())
         out.append({"d": d, "m": m, "n": n, "batch": batch, "forms": res,
                     "rel_err_split_vs_plain": err})
-        del A, X, Y, Yr, pA, pX, pY, pYr
-    # the same five shapes mixed in one call (kmx_kronmult_vmixed), against one
-    # vbatched call per shape over the same instances
+        del A, X, Y, Yr, pA, pX, pY, pYr, W
+    # the five on-chip shapes mixed in one call (kmx_kronmult_vmixed), against
+    # one vbatched call per shape over the same instances
     classes = [(m, n) for m, n, _ in cases]
     count = 40000
     rng = np.random.default_rng(SEED)
