@@ -272,33 +272,6 @@ __global__ void __launch_bounds__(NN <= 5 ? 512 : 256) grad_kernel(const GradPro
 // (so IEEE propagation and exact zeros are those of FP64).
 // ---------------------------------------------------------------------------
 
-// Running double-float sum of products of pairs.
-struct DfSum {
-  float s, c;
-  __device__ __forceinline__ void zero() { s = c = 0.f; }
-  __device__ __forceinline__ void add(df a, df b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    float t, te;
-    two_sum(s, p, t, te);
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(te, e));
-  }
-  // the sum as a normalised pair
-  __device__ __forceinline__ df pair() const {
-    df r;
-    r.hi = __fadd_rn(s, c);
-    r.lo = __fsub_rn(c, __fsub_rn(r.hi, s));
-    return r;
-  }
-  // the sum times 2^escale, in FP64
-  __device__ __forceinline__ double widen(int escale) const {
-    const df r = pair();
-    return f32_to_f64_scaled(r.hi, escale) + f32_to_f64_scaled(r.lo, escale);
-  }
-};
 
 __device__ __forceinline__ double widen_pair(df v, int escale) {
   return f32_to_f64_scaled(v.hi, escale) + f32_to_f64_scaled(v.lo, escale);

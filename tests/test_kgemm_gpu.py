@@ -4,8 +4,11 @@ outputs of the reference's own CPU build and against the oracle.  Every call
 goes through the C ABI.
 
 Tolerances:
-  FP64: normwise relative error per entry <= 1e-13 (the reference test's own
-        bound is max abs error < 1e-9, test_kgemm_nn_batched.cpp:563).
+  FP64: normwise relative error per entry <= 1e-13 on the golden inputs; on
+        random inputs (long dot products that cancel) the componentwise GEMM
+        measure |dC| <= 1e-13 (|alpha| |A||op(B)| + |beta| |C|) (the
+        reference test's own bound is max abs error < 1e-9,
+        test_kgemm_nn_batched.cpp:563).
   FP32: the reference test's max abs error < 5e-4 (:562) on its closed-form
         inputs and normwise <= 1e-5 per entry (both paths accumulate to about
         48 bits and round once).
@@ -23,6 +26,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 F64_TOL = 1e-13
+F64_CW_TOL = 1e-13  # componentwise, relative to |alpha| |A| |op(B)| + |beta| |C|
 F32_NORM_TOL = 1e-5
 F32_ABS_TOL = 5e-4
 
@@ -97,6 +101,29 @@ def test_kgemm_shared_c_golden(kmx, trans, tag):
     assert ok, err
 
 
+def _componentwise_err(trans, got, ref, A, aoff, ldA, B, boff, ldB, C0, coff, ldC, mm, nn, kk,
+                       alpha, beta):
+    """max over C elements of |got - ref| / (|alpha| (|A| |op(B)|) + |beta| |C0|):
+    the standard GEMM error measure, meaningful where a long dot product
+    cancels (a normwise relative error of a 1 x 1 output is not)."""
+    worst = 0.0
+    for b in range(len(aoff)):
+        Ab = A[aoff[b]:aoff[b] + ldA[b] * kk].reshape(kk, ldA[b]).T[:mm, :].astype(np.float64)
+        if trans == "nn":
+            Bb = B[boff[b]:boff[b] + ldB[b] * nn].reshape(nn, ldB[b]).T[:kk, :]
+        else:
+            Bb = B[boff[b]:boff[b] + ldB[b] * kk].reshape(kk, ldB[b]).T[:nn, :].T
+        Bb = Bb.astype(np.float64)
+
+        def cm(X):
+            return X[coff[b]:coff[b] + ldC[b] * nn].reshape(nn, ldC[b]).T[:mm, :].astype(np.float64)
+
+        scale = abs(alpha) * (np.abs(Ab) @ np.abs(Bb)) + abs(beta) * np.abs(cm(C0))
+        diff = np.abs(cm(got) - cm(ref))
+        worst = max(worst, float((diff / np.maximum(scale, 1e-300)).max()))
+    return worst
+
+
 def _random_case(rng, trans, T, mm, nn, kk, batch, pad):
     ldA, ldC = mm + pad, mm + pad
     ldB = (kk if trans == "nn" else nn) + pad
@@ -133,9 +160,13 @@ def test_kgemm_random_sweep_vs_oracle(kmx, oracle, trans, tag):
         assert np.array_equal(got.reshape(batch, nn, mm + 3)[:, :, mm:],
                               C.reshape(batch, nn, mm + 3)[:, :, mm:])  # padding kept
         g64, r64 = gv.astype(np.float64), rv.astype(np.float64)
-        err = blockwise_rel_err(g64, r64)
-        tol = F64_TOL if tag == "f64" else F32_NORM_TOL
-        assert err <= tol, (mm, nn, kk, err)
+        if tag == "f64":
+            err = _componentwise_err(trans, got, ref, A, aoff, ldA, B, boff, ldB, C, coff, ldC,
+                                     mm, nn, kk, 0.7, -0.4)
+            assert err <= F64_CW_TOL, (mm, nn, kk, err)
+        else:
+            err = blockwise_rel_err(g64, r64)
+            assert err <= F32_NORM_TOL, (mm, nn, kk, err)
 
 
 @pytest.mark.parametrize("beta", [0.0, 1.0, -0.4])
@@ -223,3 +254,42 @@ def test_kgemm_graph_capture_replays(kmx):
     torch.cuda.synchronize()
     err = (C - 2 * once).abs().max().item() / once.abs().max().item()
     assert err < 1e-13
+
+
+@pytest.mark.parametrize("trans", ["nn", "nt"])
+@pytest.mark.parametrize("mm,nn,kk", [(4, 1024, 4), (1024, 4, 4), (3, 5, 7), (40, 70, 20)])
+def test_kgemm_fp64_extreme_magnitudes_and_nonfinite(kmx, oracle, trans, mm, nn, kk):
+    """Entries scaled by 1e-150..1e150 stay within the FP64 bound; an Inf in
+    one entry's A and a NaN in another's B propagate as in the oracle; an
+    all-zero A gives beta * C."""
+    rng = np.random.default_rng(17 + mm)
+    batch = 6
+    args = _random_case(rng, trans, np.float64, mm, nn, kk, batch, pad=0)
+    A, aoff, ldA, B, boff, ldB, C, coff, ldC = args
+    sa = 10.0 ** rng.integers(-150, 151, batch)
+    sb = 10.0 ** rng.integers(-150, 151, batch)
+    na, nb = len(A) // batch, len(B) // batch
+    for b in range(batch):
+        A[b * na:(b + 1) * na] *= sa[b]
+        B[b * nb:(b + 1) * nb] *= sb[b]
+    C *= 1e-3
+    A[1 * na + 2] = np.inf
+    B[2 * nb + 1] = np.nan
+    A[3 * na:4 * na] = 0.0
+    ref = C.copy()
+    oracle.kgemm_batched(trans, mm, nn, kk, 1.3, A, aoff, ldA, B, boff, ldB, 1.2, ref, coff, ldC)
+    got = _run_gpu(kmx, trans, A, aoff, ldA, B, boff, ldB, C, coff, ldC, mm, nn, kk, 1.3, 1.2)
+    g2, r2 = got.reshape(batch, -1), ref.reshape(batch, -1)
+    assert np.array_equal(np.isnan(g2), np.isnan(r2))
+    assert np.array_equal(np.isinf(g2), np.isinf(r2))
+    fin = np.isfinite(r2).all(axis=1)
+    assert fin.sum() >= 4
+    idx = np.nonzero(fin)[0]
+    sub = lambda X, off, n: np.concatenate([X[off[b]:off[b] + n] for b in idx])  # noqa: E731
+    na_, nb_, nc_ = len(A) // batch, len(B) // batch, len(C) // batch
+    offs = lambda n: [i * n for i in range(len(idx))]  # noqa: E731
+    err = _componentwise_err(trans, sub(got, coff, nc_), sub(ref, coff, nc_), sub(A, aoff, na_),
+                             offs(na_), [ldA[0]] * len(idx), sub(B, boff, nb_), offs(nb_),
+                             [ldB[0]] * len(idx), sub(C, coff, nc_), offs(nc_),
+                             [ldC[0]] * len(idx), mm, nn, kk, 1.3, 1.2)
+    assert err <= F64_CW_TOL
