@@ -488,8 +488,8 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
   if (e != cudaSuccess) return cuda_fail(e);
   for (int c = 0; c < nclasses; ++c) {
     const int d = classes[2 * c], n = classes[2 * c + 1];
-    long long N;
-    ipow_checked(n, d, &N);
+    long long N = 0;
+    ipow_checked(n, d, &N);  // checked for every class above
     Problem p;
     base_square(p, L_MIXED, d, n, n, N);
     p.count = count;  // upper bound for the grid; the kernels read the class count
