@@ -362,7 +362,15 @@ int kmx_kronmult_xbatched_f64_noalloc(int d, int n, const double* const* Aarray,
 size_t kmx_deterministic_workspace_bytes(int batchCount);
 
 /* Frees the library's cached deterministic-mode workspace of the current
- * device (stream-ordered on the given stream). */
+ * device (stream-ordered on the given stream).
+ *
+ * Besides that workspace the library keeps two more per device: the grouping
+ * arrays of kmx_kronmult_mixed_* / kmx_kronmult_vmixed_* and the digits form's
+ * list of entries handed back to the double-float pass.  All three are shared
+ * by every call on the device and reallocated (stream-ordered) when a larger
+ * one is needed, so calls that use them must be ordered on the GPU (one
+ * stream, or streams joined by events); deterministic calls that overlap can
+ * pass their own kmx_options.workspace instead. */
 int kmx_release_workspace(kmx_stream_t stream);
 
 /* Reads and clears the current device's status word, written by kernels
