@@ -71,7 +71,11 @@ typedef enum kmx_form {
 typedef enum kmx_accumulate {
   KMX_ACC_ATOMIC = 0,        /* FP64/FP32 atomic add per element (reference semantics) */
   KMX_ACC_DETERMINISTIC = 1  /* entries grouped by Y block on the device, each block summed
-                                in a fixed order and written once: bitwise reproducible */
+                                in a fixed order by one group: bitwise reproducible.  Every
+                                shape of the FP64 and FP32 entry points (square n = 2..8
+                                and d >= 3 in register-tiled segment kernels, the others
+                                in the generic kernels); kmx_kronmult_xbatched_wide:
+                                register-tiled shapes only; mixed-shape calls: atomic only */
 } kmx_accumulate;
 
 /* Kernel family for square factors. */

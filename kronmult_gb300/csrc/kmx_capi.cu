@@ -176,7 +176,8 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
   if (det) {
-    if (!is_square(p) || !spec_n || p.d < 3) return KMX_ERR_UNSUPPORTED;
+    // FP32/BF16-stored inputs with FP64 Y: register-tiled segment kernels only
+    if (wide_in && (!is_square(p) || !spec_n || p.d < 3)) return KMX_ERR_UNSUPPORTED;
     const size_t need = seg_workspace_bytes(p.count);
     void* ws = o.workspace;
     size_t wsb = o.workspace_bytes;

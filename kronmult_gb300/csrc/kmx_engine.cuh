@@ -93,6 +93,40 @@ __device__ __forceinline__ long long launch_count(const Problem& p) {
   return p.count_dev ? (long long)*p.count_dev : (long long)p.count;
 }
 
+// The entries one group processes, in order: grid-stride over the launch's
+// entries (through p.order when given), or, with segments (deterministic
+// mode), every entry of each segment the group takes -- segments grid-stride
+// in the longest-first order -- in their stored order.  A segment's entries
+// share one Y block, so the group that owns it adds their contributions in a
+// fixed order (plain read-modify-write, y_exclusive).  Uniform over a group.
+struct EntryStream {
+  long long pos, step, end, obase;
+  int j, cnt, off;
+  __device__ EntryStream(const Problem& p, long long slot0, long long step_)
+      : pos(slot0), step(step_), j(0), cnt(0), off(0) {
+    end = p.seg_entries ? (long long)*p.seg_num : launch_count(p);
+    obase = p.order_base ? (long long)*p.order_base : 0;
+  }
+  __device__ bool next(const Problem& p, long long& entry) {
+    if (p.seg_entries) {
+      while (j >= cnt) {
+        if (pos >= end) return false;
+        const int sid = p.seg_order[pos];
+        off = p.seg_offset[sid];
+        cnt = p.seg_count[sid];
+        j = 0;
+        pos += step;
+      }
+      entry = p.seg_entries[off + j++];
+      return true;
+    }
+    if (pos >= end) return false;
+    entry = p.order ? (long long)p.order[obase + pos] : pos + p.entry_offset;
+    pos += step;
+    return true;
+  }
+};
+
 // ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
@@ -760,10 +794,8 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
   T* sb1 = sb0 + ((p.sxw * sizeof(T) + 15) / 16 * 16) / sizeof(T);
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
-  const long long count = launch_count(p);
-  const long long obase = p.order_base ? (long long)*p.order_base : 0;
-  for (long long e = slot0; e < count; e += step) {
-    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
+  EntryStream es(p, slot0, step);
+  for (long long entry; es.next(p, entry);) {
     EntryPtrs<T> en;
     if (!resolve_entry<T>(p, entry, en)) {
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
@@ -861,11 +893,9 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
   const bool excl = p.y_exclusive != 0;
-  const long long count = launch_count(p);
-  const long long obase = p.order_base ? (long long)*p.order_base : 0;
   const long long Nx = p.Nx;
-  for (long long e = slot0; e < count; e += step) {
-    const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
+  EntryStream es(p, slot0, step);
+  for (long long entry; es.next(p, entry);) {
     EntryPtrs<double> en;
     if (!resolve_entry<double>(p, entry, en)) {
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);

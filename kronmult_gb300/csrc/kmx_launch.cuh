@@ -225,20 +225,22 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   const DeviceInfo di = device_info(dev);
   const bool square = is_square(p);
   const int nn = p.n[0];
-  if (p.seg_entries) {
-    // deterministic mode: register-tiled segment kernels only
+  const bool seg = p.seg_entries != nullptr;
+  if (seg) {
+    // deterministic mode: the register-tiled segment kernels where they
+    // exist, else the generic kernels walking whole segments (EntryStream)
     const TileKernel tk = square ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
-    if (!tk.func) return cudaErrorNotSupported;
-    return launch_tile(p, tk, hint, stream);
+    if (tk.func) return launch_tile(p, tk, hint, stream);
   }
-  if (square && hint.engine != 1) {
+  if (!seg && square && hint.engine != 1) {
     const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
     if (tk.func) return launch_tile(p, tk, hint, stream);
   }
   if constexpr (FORM == FORM_WIDE) {
     return cudaErrorNotSupported;  // register-tiled shapes only (handled above)
   } else {
-  const bool spec = square && pick_sq<T, FORM, false>(nn) != nullptr;
+  // the square per-mode kernels take entries grid-stride only
+  const bool spec = !seg && square && pick_sq<T, FORM, false>(nn) != nullptr;
   auto group_smem = [&](bool gb) -> size_t {
     if (spec) return sq_group_smem<T, FORM>(p, gb);
     if constexpr (FORM == FORM_SPLIT) return gen_split_group_smem(p, gb, di.max_smem_optin);

@@ -269,3 +269,67 @@ def test_generic_split_transpose_option_square(kmx, oracle, d, n):
     kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", transpose=True)
     assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL
     check_status(kmx)
+
+
+@pytest.mark.parametrize("form", [None, "plain"])
+@pytest.mark.parametrize("d,m,nn,wslots", [
+    (3, [4, 5, 6], [6, 5, 4], None),
+    (6, [4, 3, 4, 3, 4, 3], [3, 4, 3, 4, 3, 4], None),
+    (2, [32, 24], [24, 32], None),
+    (5, [8, 7, 8, 7, 8], [7, 8, 7, 8, 8], 3),   # beyond shared memory: workspace slots
+])
+def test_deterministic_rectangular_vbatched(kmx, oracle, d, m, nn, wslots, form):
+    """Deterministic mode for rectangular vbatched with Y blocks shared by
+    several entries: entries grouped by Y block on the device and each block
+    summed by one group in a fixed order -- bitwise repeatable, equal to the
+    oracle."""
+    rng = np.random.default_rng(200 + d)
+    batch, nyb = 12, 4
+    Nx, Ny = int(np.prod(nn)), int(np.prod(m))
+    A, offs, X, _ = vb_case(201 + d, d, m, nn, batch=batch, y0=False)
+    yblk = rng.integers(0, nyb, batch)
+    Y0 = rng.uniform(-1, 1, (nyb, Ny))
+    Yref = Y0.copy()
+    sxw = oracle.size_xw(d, m, nn)
+    oracle.vbatched(d, m, nn, A, offs, X, [b * Nx for b in range(batch)], Yref,
+                    [int(y) * Ny for y in yblk], np.zeros(2 * sxw * batch))
+    Ad, Xd = dev(A), dev(X)
+    W = torch.zeros(2 * sxw * (wslots or batch), dtype=torch.float64, device="cuda")
+    outs = []
+    for _ in range(2):
+        Yd = dev(Y0)
+        kmx.kronmult_vbatched(d, m, nn, kmx.pointer_array(Ad, offs),
+                              kmx.pointer_array(Xd, [b * Nx for b in range(batch)]),
+                              kmx.pointer_array(Yd, [int(y) * Ny for y in yblk]), W, None, batch,
+                              form=form, accumulate="deterministic")
+        outs.append(host(Yd))
+    check_status(kmx)
+    assert np.array_equal(outs[0], outs[1])
+    assert blockwise_rel_err(outs[0], Yref) <= F64_TOL
+
+
+def test_deterministic_generic_f32(kmx, oracle):
+    """FP32 data, a shape without a tiled segment kernel (d = 2, n = 6)."""
+    rng = np.random.default_rng(301)
+    d, n, ne, nyb = 2, 6, 200, 7
+    N = n ** d
+    A = rng.standard_normal((ne, d, n, n)).astype(np.float32)
+    X = rng.standard_normal((ne, N)).astype(np.float32)
+    yblk = rng.integers(0, nyb, ne)
+    Y0 = rng.uniform(-1, 1, (nyb, N)).astype(np.float32)
+    Yref = Y0.copy()
+    # the oracle's pbatched with a Y offset per entry (it clobbers X and W)
+    offs = [b * N for b in range(ne)]
+    oracle.pbatched(d, n, A, X.copy().reshape(-1), offs, Yref.reshape(-1),
+                    [int(y) * N for y in yblk], np.zeros(ne * N, dtype=np.float32), offs)
+    Ad, Xd = dev(A), dev(X)
+    outs = []
+    for _ in range(2):
+        Yd = dev(Y0)
+        kmx.kronmult_pbatched(d, n, Ad, kmx.pointer_array(Xd, [b * N for b in range(ne)]),
+                              kmx.pointer_array(Yd, [int(y) * N for y in yblk]), None, ne,
+                              accumulate="deterministic")
+        outs.append(host(Yd))
+    check_status(kmx)
+    assert np.array_equal(outs[0], outs[1])
+    assert blockwise_rel_err(outs[0], Yref) <= 1e-5

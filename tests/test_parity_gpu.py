@@ -501,16 +501,31 @@ def test_deterministic_partial_overlap_is_refused(kmx):
     assert not Y.any()
 
 
-def test_deterministic_unsupported_shape(kmx):
-    d, n, ne = 2, 4, 3
+@pytest.mark.parametrize("form", ["auto", "plain", "split"])
+@pytest.mark.parametrize("d,n", [(2, 4), (1, 7), (3, 9), (2, 13), (2, 8)])
+def test_deterministic_shapes_without_tiled_segment_kernel(kmx, oracle, d, n, form):
+    """Shapes without a register-tiled segment kernel (d <= 2, unspecialised n):
+    the generic kernels walk whole Y segments, bitwise repeatable and equal to
+    the oracle."""
+    Apool, Xpool, Y0, y_idx, x_idx, a_idx = _pool_case(91 + d + n, d, n, pool=20, nx=16, ny=9,
+                                                       ne=300)
     N = n ** d
-    A = torch.rand((ne * d * n * n,), dtype=torch.float64, device="cuda")
-    X = torch.rand((ne, N), dtype=torch.float64, device="cuda")
-    Y = torch.zeros(N, dtype=torch.float64, device="cuda")
-    with pytest.raises(kmx.KmxError, match="UNSUPPORTED"):
-        kmx.kronmult_xbatched(d, n, kmx.pointer_array(A, [i * n * n for i in range(ne * d)]), n,
-                              kmx.pointer_array(X, [b * N for b in range(ne)]),
-                              kmx.pointer_array(Y, [0] * ne), None, ne, accumulate="deterministic")
+    ne = len(y_idx)
+    Yref = Y0.copy()
+    oracle.xbatched_idx(d, n, Apool, n, Apool.shape[1], Xpool, Yref, y_idx, x_idx, a_idx)
+    Ad, Xd = dev(Apool), dev(Xpool)
+    pool = Apool.shape[1]
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xd, x_idx * N)
+    outs = []
+    for _ in range(2):
+        Yd = dev(Y0)
+        pY = kmx.pointer_array(Yd, y_idx * N)
+        kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, ne, form=form, accumulate="deterministic")
+        outs.append(host(Yd))
+    check_status(kmx)
+    assert np.array_equal(outs[0], outs[1])
+    assert blockwise_rel_err(outs[0], Yref) <= F64_TOL
 
 
 # ---------------------------------------------------------------------------
