@@ -333,3 +333,48 @@ def test_deterministic_generic_f32(kmx, oracle):
     check_status(kmx)
     assert np.array_equal(outs[0], outs[1])
     assert blockwise_rel_err(outs[0], Yref) <= 1e-5
+
+
+def _random_shapes(seed, count):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < count:
+        d = int(rng.integers(1, 7))
+        m = [int(v) for v in rng.integers(1, 13, d)]
+        nn = [int(v) for v in rng.integers(1, 13, d)]
+        sizes = [int(np.prod(nn))] + [int(np.prod(m[:k])) * int(np.prod(nn[k:]))
+                                      for k in range(1, d + 1)]
+        if max(sizes) <= 20000:
+            out.append((d, m, nn))
+    return out
+
+
+@pytest.mark.parametrize("case", range(24))
+def test_generic_random_shape_sweep(kmx, oracle, case):
+    """Seeded random rectangular shapes (d = 1..6, extents 1..12, every
+    intermediate at most 20000 elements), random batch sizes, both FP64 forms,
+    atomic and deterministic accumulation, Y blocks shared between entries:
+    against the oracle's vbatched."""
+    d, m, nn = _random_shapes(7, 24)[case]
+    rng = np.random.default_rng(1000 + case)
+    batch = int(rng.integers(1, 9))
+    nyb = int(rng.integers(1, batch + 1))
+    Nx, Ny = int(np.prod(nn)), int(np.prod(m))
+    A, offs, X, _ = vb_case(2000 + case, d, m, nn, batch=batch, y0=False)
+    yblk = rng.integers(0, nyb, batch)
+    Y0 = rng.uniform(-1, 1, (nyb, Ny))
+    Yref = Y0.copy()
+    sxw = oracle.size_xw(d, m, nn)
+    oracle.vbatched(d, m, nn, A, offs, X, [b * Nx for b in range(batch)], Yref,
+                    [int(y) * Ny for y in yblk], np.zeros(2 * sxw * batch))
+    Ad, Xd = dev(A), dev(X)
+    W = torch.zeros(2 * sxw * batch, dtype=torch.float64, device="cuda")
+    for form in ("split", "plain"):
+        for acc in ("atomic", "deterministic"):
+            Yd = dev(Y0)
+            kmx.kronmult_vbatched(d, m, nn, kmx.pointer_array(Ad, offs),
+                                  kmx.pointer_array(Xd, [b * Nx for b in range(batch)]),
+                                  kmx.pointer_array(Yd, [int(y) * Ny for y in yblk]), W, None,
+                                  batch, form=form, accumulate=acc)
+            assert blockwise_rel_err(host(Yd), Yref) <= F64_TOL, (d, m, nn, form, acc)
+    check_status(kmx)
