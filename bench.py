@@ -418,11 +418,17 @@ def run_ours(args):
         # host wall clock from an idle pipeline: the first upload and the last
         # download are not overlapped, so average over at least 40 steps
         K2 = max(40, args.steps)
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
         for k in range(K2):
             e2e_step(k, timed=True)
         torch.cuda.synchronize()
         ms_e2e = (time.perf_counter() - t0) / K2 * 1e3
+        if dist:  # the slowest rank's step time
+            t = torch.tensor([ms_e2e], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_e2e = float(t.item())
         ms_e2e_dev = sum(a.elapsed_time(b) for a, b in cmp_events) / len(cmp_events)
         # the last step's result, read back on the host, against the device-resident run
         Ylast = Yout[(K2 - 1) % NB].to(dev)
