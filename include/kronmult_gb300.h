@@ -75,7 +75,8 @@ typedef enum kmx_accumulate {
                                 shape of the FP64 and FP32 entry points (square n = 2..8
                                 and d >= 3 in register-tiled segment kernels, the others
                                 in the generic kernels); kmx_kronmult_xbatched_wide:
-                                register-tiled shapes only; mixed-shape calls: atomic only */
+                                register-tiled shapes only; mixed-shape calls: the generic
+                                kernels, class after class over one set of segments */
 } kmx_accumulate;
 
 /* Kernel family for square factors. */
@@ -331,8 +332,8 @@ int kmx_kronmult_mixed_f32(int count, const int* dims, const float* const* Aarra
  * may repeat).  Instances with a class id outside [0, nclasses) are skipped
  * and flagged in the device status word.  Grouping, launch order and graph
  * capture as for kmx_kronmult_mixed_*; W slots of twice the class's largest
- * intermediate, for classes whose entries exceed on-chip memory.  Atomic
- * accumulation only. */
+ * intermediate, for classes whose entries exceed on-chip memory.  Atomic or
+ * deterministic accumulation (kmx_options.accumulate). */
 int kmx_kronmult_vmixed_f64(int count, const int* cls, const double* const* Aarray,
                             const long long* a_off, double* const* pX, double* const* pY,
                             double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,

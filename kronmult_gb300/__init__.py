@@ -250,7 +250,8 @@ def kronmult_xbatched_wide(d, n, Aarray, lda, pX, pY, batchCount=None, *, in_dty
 
 
 def kronmult_mixed(dims, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes=None, *,
-                   dtype=None, form=None, transpose=False, engine=None, stream=None):
+                   dtype=None, form=None, accumulate=None, transpose=False, engine=None,
+                   stream=None):
     """Instances of mixed (d, n) in one call.  dims: int32 CUDA tensor (count, 2)
     of (d, n); Aarray: factor addresses, instance i's at a_off[i] .. a_off[i]+d-1
     (a_off int64 CUDA tensor); pX/pY: block addresses; classes: host list of
@@ -265,12 +266,13 @@ def kronmult_mixed(dims, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes
     s = C.c_void_p(_stream(stream))
     fn = lib().kmx_kronmult_mixed_f64 if f64 else lib().kmx_kronmult_mixed_f32
     rc = fn(count, _addr(dims), _addr(Aarray), _addr(a_off), _addr(pX), _addr(pY), _addr(W), cap,
-            cl, len(classes), _opt(form if f64 else None, None, transpose, engine), s)
+            cl, len(classes), _opt(form if f64 else None, accumulate, transpose, engine), s)
     check(rc, "kmx_kronmult_mixed")
 
 
 def kronmult_vmixed(cls, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes=None, *,
-                    dtype=None, form=None, transpose=False, engine=None, stream=None):
+                    dtype=None, form=None, accumulate=None, transpose=False, engine=None,
+                    stream=None):
     """Instances of mixed rectangular shapes in one call.  cls: int32 CUDA tensor
     of class ids; classes: host list of (m, n) pairs of per-mode sizes (factor l
     is m[l] x n[l], leading dimension m[l]); Aarray: factor addresses,
@@ -290,7 +292,7 @@ def kronmult_vmixed(cls, Aarray, a_off, pX, pY, classes, W=None, Wcapacity_bytes
     s = C.c_void_p(_stream(stream))
     fn = lib().kmx_kronmult_vmixed_f64 if f64 else lib().kmx_kronmult_vmixed_f32
     rc = fn(count, _addr(cls), _addr(Aarray), _addr(a_off), _addr(pX), _addr(pY), _addr(W), cap,
-            cl, len(classes), _opt(form if f64 else None, None, transpose, engine), s)
+            cl, len(classes), _opt(form if f64 else None, accumulate, transpose, engine), s)
     check(rc, "kmx_kronmult_vmixed")
 
 

@@ -175,7 +175,9 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   }
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
-  if (det) {
+  if (det && p.seg_entries) {
+    p.y_exclusive = 1;  // segments prepared by the caller (mixed shapes)
+  } else if (det) {
     // FP32/BF16-stored inputs with FP64 Y: register-tiled segment kernels only
     if (wide_in && (!is_square(p) || !spec_n || p.d < 3)) return KMX_ERR_UNSUPPORTED;
     const size_t need = seg_workspace_bytes(p.count);
@@ -459,6 +461,41 @@ static int xbatched_wide_impl(int in_type, int d, int n, const void* const* Aarr
   return run_problem(p, false, o, s, in_type);
 }
 
+// Deterministic mixed-shape calls: one set of segments over every instance,
+// Y blocks of ybytes[c] bytes for class c, handed to each class's launch
+// (which takes only its own entries, EntryStream).
+template <typename T>
+static int mixed_segments(int count, T* const* pY, const MixedArrays& ma, const long long* ybytes,
+                          int nclasses, const kmx_options& o, int* status, cudaStream_t s,
+                          SegArrays* sa) {
+  const size_t need = seg_workspace_bytes(count);
+  void* ws = o.workspace;
+  size_t wsb = o.workspace_bytes;
+  if (ws == nullptr) {
+    const int rc = cached_workspace(0, need, s, &ws);
+    if (rc != KMX_OK) return rc;
+    wsb = need;
+  } else if (wsb < need) {
+    return KMX_ERR_WORKSPACE;
+  }
+  SegClassBytes cb{};
+  for (int c = 0; c < nclasses && c < 64; ++c) cb.bytes[c] = ybytes[c];
+  const cudaError_t e = seg_prepare(reinterpret_cast<void* const*>(pY), count, 0, ws, wsb, status,
+                                    s, sa, ma.keys, &cb);
+  return e == cudaSuccess ? KMX_OK : cuda_fail(e);
+}
+
+static void use_segments(Problem& p, const SegArrays& sa, const MixedArrays& ma, int c) {
+  p.seg_entries = sa.entries;
+  p.seg_offset = sa.offset;
+  p.seg_count = sa.count;
+  p.seg_order = sa.order;
+  p.seg_num = sa.num;
+  p.seg_queue = sa.queue;
+  p.seg_key = ma.keys;
+  p.seg_class = c;
+}
+
 // One call over instances of mixed (d, n): group by class on the device,
 // then one tuned launch per class reading its range from device memory.
 template <typename T>
@@ -476,7 +513,9 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
     if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
   }
   kmx_options o = resolve_options(opt);
-  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  if (o.accumulate != KMX_ACC_ATOMIC && o.accumulate != KMX_ACC_DETERMINISTIC)
+    return KMX_ERR_INVALID_ARG;
+  const bool det = o.accumulate == KMX_ACC_DETERMINISTIC;
   int* status = nullptr;
   int rc = status_ptr(&status);
   if (rc != KMX_OK) return rc;
@@ -487,12 +526,24 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
   MixedArrays ma;
   cudaError_t e = mixed_prepare(count, dims, nullptr, classes, nclasses, ws, need, status, s, &ma);
   if (e != cudaSuccess) return cuda_fail(e);
+  SegArrays sa{};
+  if (det) {
+    long long yb[KMX_MAX_CLASSES];
+    for (int c = 0; c < nclasses; ++c) {
+      long long N = 0;
+      ipow_checked(classes[2 * c + 1], classes[2 * c], &N);
+      yb[c] = N * (long long)sizeof(T);
+    }
+    rc = mixed_segments(count, pY, ma, yb, nclasses, o, status, s, &sa);
+    if (rc != KMX_OK) return rc;
+  }
   for (int c = 0; c < nclasses; ++c) {
     const int d = classes[2 * c], n = classes[2 * c + 1];
     long long N = 0;
     ipow_checked(n, d, &N);  // checked for every class above
     Problem p;
     base_square(p, L_MIXED, d, n, n, N);
+    if (det) use_segments(p, sa, ma, c);
     p.count = count;  // upper bound for the grid; the kernels read the class count
     p.count_dev = ma.counts + c;
     p.order = ma.order;
@@ -536,7 +587,9 @@ static int vmixed_impl(int count, const int* cls, const T* const* Aarray, const 
   }
   if (count == 0) return KMX_OK;
   if (!cls || !Aarray || !a_off || !pX || !pY) return KMX_ERR_NULL_POINTER;
-  if (o.accumulate != KMX_ACC_ATOMIC) return KMX_ERR_UNSUPPORTED;
+  if (o.accumulate != KMX_ACC_ATOMIC && o.accumulate != KMX_ACC_DETERMINISTIC)
+    return KMX_ERR_INVALID_ARG;
+  const bool det = o.accumulate == KMX_ACC_DETERMINISTIC;
   int* status = nullptr;
   int rc = status_ptr(&status);
   if (rc != KMX_OK) return rc;
@@ -547,10 +600,23 @@ static int vmixed_impl(int count, const int* cls, const T* const* Aarray, const 
   MixedArrays ma;
   cudaError_t e = mixed_prepare(count, nullptr, cls, nullptr, nclasses, ws, need, status, s, &ma);
   if (e != cudaSuccess) return cuda_fail(e);
+  SegArrays sa{};
+  if (det) {
+    long long yb[KMX_MAX_CLASSES];
+    for (int c = 0; c < nclasses; ++c) {
+      Problem q;
+      const int* r = classes + 13 * c;
+      rect_problem(q, L_MIXED, r[0], r + 1, r + 7, o);
+      yb[c] = q.Ny * (long long)sizeof(T);
+    }
+    rc = mixed_segments(count, pY, ma, yb, nclasses, o, status, s, &sa);
+    if (rc != KMX_OK) return rc;
+  }
   for (int c = 0; c < nclasses; ++c) {
     const int* r = classes + 13 * c;
     Problem p;
     rect_problem(p, L_MIXED, r[0], r + 1, r + 7, o);
+    if (det) use_segments(p, sa, ma, c);
     p.count = count;  // upper bound for the grid; the kernels read the class count
     p.count_dev = ma.counts + c;
     p.order = ma.order;

@@ -82,6 +82,8 @@ struct Problem {
   const int* seg_order;    // processing order of segments (longest first)
   const int* seg_num;      // number of segments (device scalar)
   int* seg_queue;          // work-queue counter, zero at launch
+  const int* seg_key;      // mixed shapes: class of each entry; only seg_class's are taken
+  int seg_class;
   // mixed-shape batches: this launch covers order[*order_base .. *order_base + *count_dev)
   const long long* a_off;  // L_MIXED: first factor pointer of instance i in A
   const int* count_dev;    // when set, the entry count is read from device memory
@@ -98,7 +100,10 @@ __device__ __forceinline__ long long launch_count(const Problem& p) {
 // mode), every entry of each segment the group takes -- segments grid-stride
 // in the longest-first order -- in their stored order.  A segment's entries
 // share one Y block, so the group that owns it adds their contributions in a
-// fixed order (plain read-modify-write, y_exclusive).  Uniform over a group.
+// fixed order (plain read-modify-write, y_exclusive).  With seg_key (mixed
+// shapes) the segments span every class and each class's launch takes only
+// its own entries; launches run class after class on the stream, so a Y
+// block's contributions still arrive in one fixed order.  Uniform over a group.
 struct EntryStream {
   long long pos, step, end, obase;
   int j, cnt, off;
@@ -109,16 +114,18 @@ struct EntryStream {
   }
   __device__ bool next(const Problem& p, long long& entry) {
     if (p.seg_entries) {
-      while (j >= cnt) {
-        if (pos >= end) return false;
-        const int sid = p.seg_order[pos];
-        off = p.seg_offset[sid];
-        cnt = p.seg_count[sid];
-        j = 0;
-        pos += step;
+      for (;;) {
+        while (j >= cnt) {
+          if (pos >= end) return false;
+          const int sid = p.seg_order[pos];
+          off = p.seg_offset[sid];
+          cnt = p.seg_count[sid];
+          j = 0;
+          pos += step;
+        }
+        entry = p.seg_entries[off + j++];
+        if (!p.seg_key || p.seg_key[entry] == p.seg_class) return true;
       }
-      entry = p.seg_entries[off + j++];
-      return true;
     }
     if (pos >= end) return false;
     entry = p.order ? (long long)p.order[obase + pos] : pos + p.entry_offset;

@@ -34,7 +34,8 @@ TcKernel pick_tc(int n, int d) {
 
 template <typename In, typename Out>
 cudaError_t launch_tc(Problem& p, cudaStream_t s) {
-  if (!is_square(p)) return cudaErrorNotSupported;
+  // class-filtered segments (deterministic mixed shapes): generic kernels only
+  if (!is_square(p) || p.seg_key) return cudaErrorNotSupported;
   const TcKernel k = p.seg_entries ? pick_tc<In, Out, true>(p.n[0], p.d)
                                    : pick_tc<In, Out, false>(p.n[0], p.d);
   if (!k.func) return cudaErrorNotSupported;

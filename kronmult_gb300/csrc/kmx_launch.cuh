@@ -229,7 +229,8 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   if (seg) {
     // deterministic mode: the register-tiled segment kernels where they
     // exist, else the generic kernels walking whole segments (EntryStream)
-    const TileKernel tk = square ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
+    // (class-filtered segments of mixed-shape calls: generic kernels only)
+    const TileKernel tk = square && !p.seg_key ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
     if (tk.func) return launch_tile(p, tk, hint, stream);
   }
   if (!seg && square && hint.engine != 1) {

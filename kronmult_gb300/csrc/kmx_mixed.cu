@@ -141,6 +141,7 @@ cudaError_t mixed_prepare(int count, const int* dims, const int* cls, const int*
   class_range_kernel<<<1, KMX_MAX_CLASSES + 1, 0, s>>>(skeys, count, nclasses, offsets, counts);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  out->keys = keys;
   out->order = order;
   out->offsets = offsets;
   out->counts = counts;

@@ -8,6 +8,7 @@
 namespace kmx {
 
 struct MixedArrays {
+  const int* keys;     // class of each instance (nclasses: not in the list)
   const int* order;    // instance ids sorted by class (stable)
   const int* offsets;  // first position of class c in order[] (device)
   const int* counts;   // instances of class c (device)

@@ -34,14 +34,25 @@ __global__ void seg_keys_kernel(void* const* pY, int B, unsigned long long* keys
 
 // Y blocks of consecutive segments must not overlap.  One block; on
 // overlap the segment count is zeroed so the compute kernel does nothing.
+// With entry classes, a segment's block is as long as the longest block of its
+// entries (blocks of different classes may start at one address).
 __global__ void seg_check_kernel(const unsigned long long* uniq, int* num, long long ybytes,
-                                 int* status) {
+                                 const int* entries, const int* offsets, const int* counts,
+                                 const int* entry_class, SegClassBytes classes, int* status) {
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   const int n = *num;
   for (int s = threadIdx.x; s + 1 < n; s += blockDim.x) {
-    if ((long long)(uniq[s + 1] - uniq[s]) < ybytes) bad = 1;
+    long long len = ybytes;
+    if (entry_class) {
+      len = 0;
+      for (int j = offsets[s]; j < offsets[s] + counts[s]; ++j) {
+        const int c = entry_class[entries[j]];
+        if (c >= 0 && c < 64 && classes.bytes[c] > len) len = classes.bytes[c];
+      }
+    }
+    if ((long long)(uniq[s + 1] - uniq[s]) < len) bad = 1;
   }
   __syncthreads();
   if (threadIdx.x == 0 && bad) {
@@ -102,7 +113,8 @@ SegLayout seg_layout(int B) {
 size_t seg_workspace_bytes(int B) { return seg_layout(B).total; }
 
 cudaError_t seg_prepare(void* const* pY, int B, long long ybytes, void* ws, size_t ws_bytes,
-                        int* status, cudaStream_t s, SegArrays* out) {
+                        int* status, cudaStream_t s, SegArrays* out, const int* entry_class,
+                        const SegClassBytes* classes) {
   const SegLayout L = seg_layout(B);
   if (ws == nullptr || ws_bytes < L.total) return cudaErrorInvalidValue;
   unsigned char* w = static_cast<unsigned char*>(ws);
@@ -135,7 +147,10 @@ cudaError_t seg_prepare(void* const* pY, int B, long long ybytes, void* ws, size
     return e;
   tb = L.temp_bytes;
   if ((e = cub::DeviceScan::ExclusiveSum(temp, tb, counts, offsets, B, s)) != cudaSuccess) return e;
-  seg_check_kernel<<<1, 1024, 0, s>>>(uniq, num, ybytes, status);
+  SegClassBytes cb{};
+  if (entry_class && classes) cb = *classes;
+  seg_check_kernel<<<1, 1024, 0, s>>>(uniq, num, ybytes, entries, offsets, counts,
+                                      classes ? entry_class : nullptr, cb, status);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   int bits = 1;
   while (bits < 31 && (1LL << bits) <= (long long)B) ++bits;

@@ -17,9 +17,16 @@ struct SegArrays {
 // Bytes of workspace seg_prepare needs for B entries.
 size_t seg_workspace_bytes(int B);
 
+// Y block sizes per entry class (mixed-shape calls), at most 64 classes.
+struct SegClassBytes {
+  long long bytes[64];
+};
+
 // Build the segments of B entries whose Y blocks are pY[0..B-1] (each ybytes
-// long) in workspace ws, asynchronously on stream s.
+// long; or, with entry_class, classes->bytes[entry_class[e]] long) in
+// workspace ws, asynchronously on stream s.
 cudaError_t seg_prepare(void* const* pY, int B, long long ybytes, void* ws, size_t ws_bytes,
-                        int* status, cudaStream_t s, SegArrays* out);
+                        int* status, cudaStream_t s, SegArrays* out,
+                        const int* entry_class = nullptr, const SegClassBytes* classes = nullptr);
 
 }  // namespace kmx

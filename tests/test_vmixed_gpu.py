@@ -201,3 +201,104 @@ def test_vmixed_missing_workspace_for_large_class(kmx):
     dv = _device(kmx, cs, classes)
     with pytest.raises(kmx.KmxError):
         kmx.kronmult_vmixed(dv["cls"], dv["pA"], dv["a_off"], dv["pX"], dv["pY"], classes, None)
+
+
+def _shared_y_case(seed, classes, count, blocks_per_size, sizes, rng_dtype=np.float64):
+    """Instances of random classes whose Y blocks come from one pool per block
+    size, so that instances of one class -- and of different classes with
+    equal block sizes -- add into the same block."""
+    rng = np.random.default_rng(seed)
+    cls = rng.integers(0, len(classes), count).astype(np.int32)
+    pools, o = {}, 0
+    for sz in sorted(set(sizes)):
+        pools[sz] = [o + k * sz for k in range(blocks_per_size)]
+        o += blocks_per_size * sz
+    Y0 = rng.uniform(-1, 1, o)
+    yoff = [int(rng.choice(pools[sizes[c]])) for c in cls]
+    return cls, Y0, yoff, rng
+
+
+def _run_twice(call, Y0):
+    outs = []
+    for _ in range(2):
+        Yd = torch.from_numpy(Y0.copy()).cuda()
+        call(Yd)
+        torch.cuda.synchronize()
+        outs.append(Yd.cpu().numpy())
+    return outs
+
+
+def test_mixed_square_deterministic_vs_oracle(kmx, oracle):
+    """kmx_kronmult_mixed_f64, deterministic: instances of several (d, n)
+    classes share Y blocks (also across classes of equal block size); the
+    result is bitwise repeatable and equals the oracle's contributions summed
+    per block."""
+    classes = [(2, 4), (4, 2), (3, 4), (6, 2), (2, 8), (1, 16), (5, 3)]
+    sizes = [n ** d for d, n in classes]
+    cls, Y0, yoff, rng = _shared_y_case(11, classes, 400, 6, sizes)
+    factors, xs, ptr_offs, aoff, xoff, dims = [], [], [], [], [], []
+    Yref = Y0.copy()
+    fo = xo = 0
+    for i, c in enumerate(cls):
+        d, n = classes[c]
+        dims.append((d, n))
+        A = rng.standard_normal((1, d, n, n)) / np.sqrt(n)
+        X = rng.standard_normal((1, n ** d))
+        contrib = np.zeros_like(X)
+        oracle.batched(d, n, A, X.copy(), contrib, np.zeros_like(X), 1)
+        Yref[yoff[i]:yoff[i] + n ** d] += contrib[0]
+        aoff.append(len(ptr_offs))
+        ptr_offs += [fo + l * n * n for l in range(d)]  # factor l of instance i
+        factors.append(A.reshape(-1))
+        fo += d * n * n
+        xs.append(X.reshape(-1))
+        xoff.append(xo)
+        xo += n ** d
+    fbuf = torch.from_numpy(np.concatenate(factors)).cuda()
+    xbuf = torch.from_numpy(np.concatenate(xs)).cuda()
+    pA = kmx.pointer_array(fbuf, ptr_offs)
+    pX = kmx.pointer_array(xbuf, xoff)
+    dims_d = torch.from_numpy(np.array(dims, dtype=np.int32)).cuda()
+    a_off = torch.tensor(aoff, dtype=torch.int64, device="cuda")
+
+    def call(Yd):
+        kmx.kronmult_mixed(dims_d, pA, a_off, pX, kmx.pointer_array(Yd, yoff), classes, None,
+                           accumulate="deterministic")
+
+    outs = _run_twice(call, Y0)
+    assert kmx.check_device_status() == 0
+    assert np.array_equal(outs[0], outs[1])
+    rows = sorted(set((o, sizes[c]) for o, c in zip(yoff, cls)))
+    worst = max(blockwise_rel_err(outs[0][o:o + sz][None, :], Yref[o:o + sz][None, :])
+                for o, sz in rows)
+    assert worst <= F64_TOL
+
+
+@pytest.mark.parametrize("form", [None, "plain"])
+def test_vmixed_deterministic_vs_oracle(kmx, oracle, form):
+    """kmx_kronmult_vmixed_f64, deterministic, rectangular classes (one beyond
+    shared memory) sharing Y blocks, also across classes of equal block size:
+    bitwise repeatable, equal to the oracle's vbatched run class by class."""
+    classes = [([4, 3], [3, 4]), ([3, 4], [5, 2]), ([4, 3, 4], [3, 4, 3]),
+               ([2, 3, 8], [3, 4, 4]), ([8, 7, 8, 7, 8], [7, 8, 7, 8, 8])]
+    sizes = [int(np.prod(m)) for m, _ in classes]
+    cs = _case(13, classes, 300, big_share=0.02)
+    rng = np.random.default_rng(14)
+    pools, o = {}, 0
+    for sz in sorted(set(sizes)):
+        pools[sz] = [o + k * sz for k in range(5)]
+        o += 5 * sz
+    cs["Y0"] = rng.uniform(-1, 1, o)
+    cs["yoff"] = [int(rng.choice(pools[sizes[c]])) for c in cs["cls"]]
+    ref = _oracle(oracle, classes, cs)
+    dv = _device(kmx, cs, classes)
+
+    def call(Yd):
+        kmx.kronmult_vmixed(dv["cls"], dv["pA"], dv["a_off"], dv["pX"],
+                            kmx.pointer_array(Yd, cs["yoff"]), classes, dv["W"], form=form,
+                            accumulate="deterministic")
+
+    outs = _run_twice(call, cs["Y0"])
+    assert kmx.check_device_status() == 0
+    assert np.array_equal(outs[0], outs[1])
+    assert _err(outs[0], ref, cs, classes) <= F64_TOL
