@@ -312,7 +312,9 @@ int kmx_kronmult_batched_grad_f32(int d, int n, const float* A, const float* X, 
  * class runs its tuned kernel, in the order of the class list, without a host
  * synchronisation (the call can be captured in a CUDA graph after one warm-up
  * call).  W (Wcapacity_bytes) is needed only by classes whose entries exceed
- * on-chip memory (slots of 2*n^d elements). */
+ * on-chip memory (slots of 2*n^d elements).  With deterministic accumulation
+ * every class runs a generic kernel over one set of Y segments (slower than
+ * the tuned kernels, bitwise reproducible). */
 int kmx_kronmult_mixed_f64(int count, const int* dims, const double* const* Aarray,
                            const long long* a_off, double* const* pX, double* const* pY,
                            double* W, size_t Wcapacity_bytes, const int* classes, int nclasses,
