@@ -160,3 +160,20 @@ def test_vmixed_argument_checks_without_gpu(kmx):
         assert fn(-1, 8, 8, 8, 8, 8, 0, 0, good, 1, None, None) == 1  # negative count
         assert fn(4, 0, 8, 8, 8, 8, 0, 0, good, 1, None, None) == 2   # no class ids
         assert fn(0, 0, 0, 0, 0, 0, 0, 0, good, 1, None, None) == 0   # empty call
+
+
+def test_grad_ex_and_mixed_accumulate_checks_without_gpu(kmx):
+    from kronmult_gb300 import _lib
+
+    L = kmx.lib()
+    bad_form = _lib.options(7)  # no such form
+    assert L.kmx_kronmult_batched_grad_f64_ex(3, 4, 8, 8, 8, 0, 8, 8, 0, 0, 2, C.byref(bad_form),
+                                              None) == 1
+    assert L.kmx_kronmult_batched_grad_f64_ex(0, 4, 8, 8, 8, 0, 8, 8, 0, 0, 2, None, None) == 1
+    assert L.kmx_kronmult_batched_grad_f64_ex(3, 4, 0, 8, 8, 0, 8, 8, 0, 0, 2, None, None) == 2
+    assert L.kmx_kronmult_batched_grad_f64_ex(3, 4, 8, 8, 8, 0, 8, 8, 0, 0, 0, None, None) == 0
+    bad_acc = _lib.options("auto", 5)  # no such accumulation mode
+    good = (C.c_int * 13)(2, 3, 4, 1, 1, 1, 1, 4, 5, 1, 1, 1, 1)
+    assert L.kmx_kronmult_vmixed_f64(4, 8, 8, 8, 8, 8, 0, 0, good, 1, C.byref(bad_acc), None) == 1
+    sq = (C.c_int * 2)(3, 4)
+    assert L.kmx_kronmult_mixed_f64(4, 8, 8, 8, 8, 8, 0, 0, sq, 1, C.byref(bad_acc), None) == 1
