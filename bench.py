@@ -87,22 +87,22 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profile_value(name, key):
-    """A `key = value` line of a committed ncu summary (profiles/), or None."""
-    p = os.path.join(ROOT, "profiles", name)
+def profile_value(key):
+    """A per-entry ncu counter of the headline kernel, from the committed
+    profiles/kernel_counters.json (each value names the capture it comes
+    from), or None."""
+    p = os.path.join(ROOT, "profiles", "kernel_counters.json")
     try:
         with open(p) as f:
-            for line in f:
-                if line.startswith(key):
-                    return float(line.split("=")[1].split()[0])
-    except (OSError, ValueError, IndexError):
-        pass
-    return None
+            v = json.load(f)["xbatched_d6n4_split"][key]
+        return float(v)
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
 
 
 def profile_traffic():
-    """DRAM bytes per entry of the split kernel from the committed ncu summary."""
-    return profile_value("xbatched_d6n4_traffic.txt", "dram_bytes_per_entry")
+    """DRAM bytes per entry of the split kernel (one full-size ncu capture)."""
+    return profile_value("dram_bytes_per_entry")
 
 
 class ClockSampler:
@@ -481,7 +481,7 @@ def run_ours(args):
     # instructions per entry from the committed ncu summary of the kernel;
     # peak = 4 schedulers x SMs x the SM clock sampled in the timed region.
     issue = None
-    ipe = profile_value("xbatched_d6n4_split_tile_kernel.md", "warp_instructions_per_entry")
+    ipe = profile_value("warp_instructions_per_entry")
     sm_mhz = (clocks or {}).get("sm_mhz")
     if ipe and sm_mhz:
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -491,7 +491,7 @@ def run_ours(args):
                  "instructions_per_entry": ipe, "achieved": float(f"{ach:.4g}"),
                  "peak": float(f"{peak:.4g}"), "frac": round(ach / peak, 3),
                  "source": "ncu smsp__inst_executed.sum of the kernel "
-                           "(profiles/xbatched_d6n4_split_tile_kernel.md)"}
+                           "(profiles/kernel_counters.json)"}
 
     cpu = None if args.no_cpu_baseline else cpu_baseline(w)
     line = {
@@ -756,7 +756,10 @@ def run_precision(args):
         pA32 = ((lvl * pool + ai) * (n * n * 4) + A32.data_ptr()).reshape(-1).contiguous()
         pX32 = xi * (N * 4) + X32.data_ptr()
         pY32 = yi * (N * 4) + Y32.data_ptr()
-        for name, fm in (("f32_y32", None), ("f32_y32_tf32x3", "tf32x3")):
+        # f32_y32: the default FP32 form (each dot product rounded once, the
+        # reference's float semantics); _fma: FP32 fused multiply-add
+        for name, fm in (("f32_y32", None), ("f32_y32_fma", "plain"),
+                         ("f32_y32_tf32x3", "tf32x3")):
             call = lambda: kmx.kronmult_xbatched(d, n, pA32, n, pX32, pY32, None, entries,
                                                  dtype=torch.float32, form=fm)
             ms = _events_time(torch, call, max(3, args.steps // 2), 2)

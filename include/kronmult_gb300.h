@@ -13,6 +13,11 @@
  *   - calls are asynchronous on the given stream (0 = legacy default stream);
  *     the caller synchronises, as with the reference (test_kronmult6_batched.cpp:248).
  *
+ * The library looks up the device addresses of its own device variables (the
+ * status word, the diagnostic counters, the no-allocation scratch) once per
+ * device and keeps them for the life of the process: do not use it across a
+ * cudaDeviceReset of a device it has run on.
+ *
  * Differences from the reference, all supersets of its contract:
  *   - each call returns a kmx_status instead of asserting;
  *   - X is never modified (the reference may clobber X in batched/pbatched);
@@ -43,23 +48,31 @@ typedef enum kmx_status {
                                 through the device status word, bit 16) */
 } kmx_status;
 
-/* Arithmetic form.  FP64 entry points: AUTO, PLAIN, SPLIT, DIGITS (the fused
- * backward: PLAIN runs FP64, the others double-float).  FP32-stored entry
- * points (the _f32 functions and kmx_kronmult_xbatched_wide): FP32 fused
- * multiply-add unless TF32X3 is asked for. */
+/* Arithmetic form.  FP64 entry points: AUTO, PLAIN, SPLIT, SPLIT_RAW, DIGITS
+ * (the fused backward: PLAIN runs FP64, the others double-float).  FP32 entry
+ * points (the _f32 functions): AUTO and SPLIT round each dot product once, as
+ * the reference's float kernels do; PLAIN is FP32 fused multiply-add; TF32X3
+ * the tensor cores.  kmx_kronmult_xbatched_wide: FP32 fused multiply-add
+ * unless TF32X3 is asked for. */
 typedef enum kmx_form {
   KMX_FORM_AUTO = 0,   /* square shapes: per-(d,n) choice from the tuning table;
                           other shapes: SPLIT once an X or Y block has 512 or more
                           elements, PLAIN below */
   KMX_FORM_PLAIN = 1,  /* native FP64 fused multiply-add */
   KMX_FORM_SPLIT = 2,  /* double-float: FP64 values carried as FP32 (hi, lo) pairs,
-                          ~2^-47 relative per operation, FP64 in and out */
+                          ~2^-48 relative to |K||X| per entry, FP64 in and out.  An entry
+                          whose result cancels (rho_F = ||KX|| sqrt(prod n_l) /
+                          (prod ||A_l||_F ||X||) below 1/4) is recomputed in FP64, so the
+                          form is as accurate as PLAIN wherever PLAIN holds 1e-13
+                          (kmx_read_redo_counters counts those entries) */
   KMX_FORM_DIGITS = 4, /* FP64 data on the FP16 tensor cores: X and factors as 7 base-2^9
                           digits with one exponent per entry, exact digit products
                           (mma.sync), exact FP32 level sums, FP64 out.  Square n = 4
                           (d = 4, 6) and n = 16 (d = 2, 3), atomic mode; entries whose
                           result falls far below the entry's scale, or with Inf/NaN, are
                           recomputed in double-float.  Other shapes: SPLIT. */
+  KMX_FORM_SPLIT_RAW = 5, /* SPLIT without the cancellation guard (accuracy studies):
+                             error about 2^-48 ||(|K||X|)|| */
   KMX_FORM_TF32X3 = 3  /* FP32-stored data only: tensor cores (mma.sync TF32), each
                           operand split into two TF32 parts, three products, FP32
                           accumulation (~2^-21 relative per product).  Square n = 4
@@ -134,7 +147,15 @@ int kmx_kronmult_vbatched_f64(int d, const int* m, const int* n, const double* c
                               size_t Wcapacity_bytes, int batchCount, kmx_stream_t stream);
 
 /* FP32 storage forms of the same four entry points (the reference's float
- * templates).  Arithmetic is FP32 fused multiply-add. */
+ * templates).  By default (form AUTO or SPLIT) each dot product is formed from
+ * exact products summed as an FP32 pair and rounded once to FP32, stage by
+ * stage in the reference's mode order (A1 first), which is what the
+ * reference's float kernels compute by accumulating in double
+ * (kgemm_nt.hpp:557-571, kgemm_nn.hpp:688-701): results agree with its float
+ * build to within one FP32 ulp per element where the summation order of
+ * overlapping Y blocks is the same (deterministic mode).  _ex with form PLAIN
+ * runs FP32 fused multiply-add instead (faster, ~2^-24 per product), TF32X3
+ * the tensor cores. */
 int kmx_kronmult_batched_f32(int d, int n, const float* A, float* X, float* Y, float* W,
                              int batchCount, kmx_stream_t stream);
 int kmx_kronmult_pbatched_f32(int d, int n, const float* A, float* const* pX, float* const* pY,
@@ -357,16 +378,24 @@ void kmx_get_default_options(kmx_options* opt);
  * callers that cannot allocate device memory.  No counterpart in the
  * reference.  Its sort and segment scratch is a fixed 16 MiB array in the
  * library's device image (per GPU, held until exit); batches whose scratch
- * exceeds it return KMX_ERR_WORKSPACE before any launch.  The first call on a
- * device looks the array up (cudaGetSymbolAddress): make it before any stream
- * capture.  All calls share the array, so calls overlapping on the GPU race.
- * Shapes: square n = 2..8, d = 3..6 (entries that fit on chip). */
+ * exceeds it return KMX_ERR_WORKSPACE before any launch.  Shapes: any square
+ * shape whose entry fits in on-chip memory; one that would need a global
+ * workspace for its intermediate (n = 8 with d >= 5, for example) returns
+ * KMX_ERR_UNSUPPORTED, also before any launch.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress) and keeps the address for the
+ * life of the device's primary context: make that call before any stream
+ * capture, and do not use the library across cudaDeviceReset.  All calls
+ * share the array, so calls overlapping on the GPU race. */
 int kmx_kronmult_xbatched_f64_noalloc(int d, int n, const double* const* Aarray, int lda,
                                       double* const* pX, double* const* pY, int batchCount,
                                       kmx_stream_t stream);
 
 /* Device workspace the deterministic mode needs for batchCount entries. */
 size_t kmx_deterministic_workspace_bytes(int batchCount);
+
+/* Bytes the library currently holds in its cached workspaces on the current
+ * device (see kmx_release_workspace); 0 when none was ever needed. */
+size_t kmx_cached_workspace_bytes(void);
 
 /* Frees the library's cached deterministic-mode workspace of the current
  * device (stream-ordered on the given stream).
@@ -385,6 +414,15 @@ int kmx_release_workspace(kmx_stream_t stream);
  * Synchronises the stream.  Returns KMX_OK or KMX_ERR_DEVICE; *flags gets
  * the raw bits (may be NULL). */
 int kmx_check_device_status(kmx_stream_t stream, int* flags);
+
+/* Reads and clears the current device's diagnostic counters (no counterpart
+ * in the reference).  counts[0]: entries of the double-float forms that the
+ * cancellation guard recomputed in plain FP64 (an entry whose
+ * rho_F = ||KX|| sqrt(prod n_l) / (prod_l ||A_l||_F ||X||) falls below 1/4,
+ * where double-float's ~2^-48 relative to |K||X| would lose more accuracy than
+ * FP64); counts[1]: entries the digits form handed to the double-float pass.
+ * Synchronises the stream; counts may be NULL (then only cleared). */
+int kmx_read_redo_counters(kmx_stream_t stream, unsigned long long* counts);
 
 /* The last CUDA error code seen by the library on this thread. */
 int kmx_last_cuda_error(void);

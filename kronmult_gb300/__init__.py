@@ -94,6 +94,16 @@ def check_device_status(stream=None) -> int:
     return flags.value
 
 
+def read_redo_counters(stream=None) -> tuple[int, int]:
+    """Read and clear the device's diagnostic counters: (entries the
+    cancellation guard recomputed in FP64, digits-form entries handed to the
+    double-float pass)."""
+    c = (C.c_ulonglong * 2)()
+    rc = lib().kmx_read_redo_counters(C.c_void_p(_stream(stream)), c)
+    check(rc, "kmx_read_redo_counters")
+    return int(c[0]), int(c[1])
+
+
 def _opt(form, accumulate, transpose, engine=None, workspace=None):
     if form is None and accumulate is None and not transpose and engine is None:
         return None
@@ -112,7 +122,7 @@ def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accum
         rc = L.kmx_kronmult_batched_f64_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
                                            _opt(form, accumulate, transpose, engine), s)
     else:
-        if form not in (None, "auto", "plain"):
+        if form not in (None, "auto", "plain", "split", "tf32x3"):
             raise KmxError(4, "kmx_kronmult_batched_f32")
         rc = L.kmx_kronmult_batched_f32_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
                                            _opt(form, accumulate, transpose, engine), s)

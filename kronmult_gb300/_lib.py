@@ -27,7 +27,7 @@ STATUS = {
     7: "KMX_ERR_OVERLAP",
 }
 
-FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3, "digits": 4}
+FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3, "digits": 4, "split_raw": 5}
 ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2}
 ACCUMULATE = {"atomic": 0, "deterministic": 1}
 
@@ -72,6 +72,7 @@ _SIGS = {
     "kmx_kronmult_xbatched_f32_ex": [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _optp, _vp],
     "kmx_kronmult_vbatched_f32_ex": [_i, _ip, _ip, _vp, _vp, _vp, _vp, _sz, _i, _optp, _vp],
     "kmx_check_device_status": [_vp, _ip],
+    "kmx_read_redo_counters": [_vp, C.POINTER(C.c_ulonglong)],
     "kmx_last_cuda_error": [],
     "kmx_probe_fma_rate": [_i, C.POINTER(C.c_double)],
     "kmx_release_workspace": [_vp],
@@ -138,6 +139,8 @@ def lib():
             L.kmx_xbatched_build_workspace_bytes.restype = _sz
             L.kmx_xbatched_build_workspace_bytes.argtypes = [_i]
             L.kmx_deterministic_workspace_bytes.restype = C.c_size_t
+            L.kmx_cached_workspace_bytes.argtypes = []
+            L.kmx_cached_workspace_bytes.restype = C.c_size_t
             L.kmx_version.argtypes = []
             L.kmx_version.restype = C.c_char_p
             _lib = L

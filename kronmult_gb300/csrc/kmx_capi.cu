@@ -21,6 +21,11 @@ namespace kmx {
 // kmx_check_device_status.
 __device__ int g_status_word;
 
+// Diagnostic counters (kmx_read_redo_counters): [0] double-float entries the
+// cancellation guard recomputed in FP64, [1] digits-form entries handed to the
+// double-float pass.
+__device__ unsigned long long g_redo_words[2];
+
 namespace {
 
 constexpr int MAX_DEVICES = 64;
@@ -30,6 +35,7 @@ std::mutex g_mu;
 DeviceInfo g_dev[MAX_DEVICES];
 bool g_dev_ok[MAX_DEVICES];
 int* g_status_ptr[MAX_DEVICES];
+unsigned long long* g_redo_ptr[MAX_DEVICES];
 std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 
 kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
@@ -77,6 +83,22 @@ int status_ptr(int** out) {
     g_status_ptr[dev] = static_cast<int*>(p);
   }
   *out = g_status_ptr[dev];
+  return KMX_OK;
+}
+
+int redo_ptr(unsigned long long** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e);
+  if (dev < 0 || dev >= MAX_DEVICES) return KMX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_redo_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_redo_words);
+    if (e != cudaSuccess) return cuda_fail(e);
+    g_redo_ptr[dev] = static_cast<unsigned long long*>(p);
+  }
+  *out = g_redo_ptr[dev];
   return KMX_OK;
 }
 
@@ -156,6 +178,26 @@ static int tuned_form(int d, int n) {
   return 0;
 }
 
+// The FP64 form a call runs: SPLIT_RAW is SPLIT without the guard; AUTO
+// takes the tuning table's choice for square shapes, else double-float once
+// an X or Y block has 512 elements (below that its per-entry scaling costs
+// more than FP64 does).
+static int resolve_f64_form(const Problem& p, int form) {
+  if (form == KMX_FORM_SPLIT_RAW) return KMX_FORM_SPLIT;
+  if (form != KMX_FORM_AUTO) return form;
+  const bool sq = is_square(p);
+  const bool spec_n = (p.n[0] >= 2 && p.n[0] <= 8) || p.n[0] == 16;
+  const int t = sq ? tuned_form(p.d, p.n[0]) : 0;
+  const bool gen_split = p.Nx >= 512 || p.Ny >= 512;
+  return t ? t : (((sq && spec_n) || gen_split) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
+}
+
+// The tuned engine for an FP64 form on square shapes (0 = choose).
+static int f64_engine(const Problem& p, int form, int engine) {
+  if (engine || !is_square(p)) return engine;
+  return tuned_engine((form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1, p.d, p.n[0]);
+}
+
 // ---------------------------------------------------------------------------
 // Common driver: validated Problem -> launcher of the requested form.
 // ---------------------------------------------------------------------------
@@ -175,6 +217,15 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   }
   int rc = status_ptr(&p.status);
   if (rc != KMX_OK) return rc;
+  rc = redo_ptr(&p.redo_ctr);
+  if (rc != KMX_OK) return rc;
+  // Test hook: KMX_TEST_EXPIRE_WAITS=1 makes the register-tiled kernels'
+  // first wait on a staged X block report a timeout (the copy is drained and
+  // DF_WAIT_TIMEOUT set, as when a wait really runs out).  Read on every call.
+  {
+    const char* w = std::getenv("KMX_TEST_EXPIRE_WAITS");
+    p.wait_expire = (w && w[0] == '1') ? 1 : 0;
+  }
   if (det && p.seg_entries) {
     p.y_exclusive = 1;  // segments prepared by the caller (mixed shapes)
   } else if (det) {
@@ -217,25 +268,26 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     if (e == cudaErrorNotSupported)
       e = wide_in == KMX_IN_BF16 ? launch_wide_bf16(p, h, s) : launch_wide_f32(p, h, s);
   } else if (!is_f64) {
+    // FP32 data.  AUTO / SPLIT: the reference's float semantics (each dot
+    // product accumulated exactly enough and rounded once, stage by stage in
+    // its mode order); PLAIN: FP32 fused multiply-add (fastest); TF32X3:
+    // tensor cores where a kernel exists, else PLAIN.
     e = cudaErrorNotSupported;
     if (o.form == KMX_FORM_TF32X3) e = launch_tc_f32(p, s);
     if (e == cudaErrorNotSupported) {
-      if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
-      e = launch_f32_plain(p, h, s);
+      if (o.form == KMX_FORM_AUTO || o.form == KMX_FORM_SPLIT) {
+        e = launch_f32_ref(p, h, s);
+      } else if (o.form == KMX_FORM_PLAIN || o.form == KMX_FORM_TF32X3) {
+        if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
+        e = launch_f32_plain(p, h, s);
+      } else {
+        return KMX_ERR_INVALID_ARG;
+      }
     }
   } else {
-    int form = o.form;
-    if (form == KMX_FORM_AUTO) {
-      const int t = sq ? tuned_form(p.d, p.n[0]) : 0;
-      // double-float wherever it measured faster: the specialised square
-      // kernels, and the generic kernel once an entry has 512 elements
-      // (below that its per-entry scaling costs more than FP64 does)
-      const bool gen_split = p.Nx >= 512 || p.Ny >= 512;
-      form = t ? t : (((sq && spec_n) || gen_split) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
-    }
-    if (h.engine == 0 && sq)
-      h.engine = tuned_engine((form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1, p.d,
-                              p.n[0]);
+    if (o.form == KMX_FORM_SPLIT_RAW) p.guard_off = 1;
+    int form = resolve_f64_form(p, o.form);
+    h.engine = f64_engine(p, form, h.engine);
     if (form == KMX_FORM_DIGITS) {
       e = cudaErrorNotSupported;
       if (digits_supported(p)) {
@@ -261,6 +313,24 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   if (e == cudaErrorInvalidValue) return KMX_ERR_WORKSPACE;
   if (e == cudaErrorNotSupported) return KMX_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e);
+  return KMX_OK;
+}
+
+static void base_square(Problem& p, int layout, int d, int n, int ld, long long N);
+
+int xbatched_f64_plan(int d, int n, int lda, int form, int accumulate, bool* needs_ws) {
+  if (d < 1 || d > MAXD || n < 1) return KMX_ERR_INVALID_ARG;
+  if (lda == 0) lda = n;
+  if (lda < n) return KMX_ERR_INVALID_ARG;
+  long long N;
+  if (!ipow_checked(n, d, &N)) return KMX_ERR_UNSUPPORTED;
+  Problem p;
+  base_square(p, L_XBATCHED, d, n, lda, N);
+  const int f = resolve_f64_form(p, form);
+  const bool seg = accumulate == KMX_ACC_DETERMINISTIC;
+  const int engine = f64_engine(p, f, 0);
+  *needs_ws = (f == KMX_FORM_PLAIN) ? needs_workspace_f64_plain(p, seg, engine)
+                                    : needs_workspace_f64_split(p, seg, engine);
   return KMX_OK;
 }
 
@@ -777,6 +847,15 @@ size_t kmx_deterministic_workspace_bytes(int batchCount) {
   return batchCount > 0 ? seg_workspace_bytes(batchCount) : 0;
 }
 
+size_t kmx_cached_workspace_bytes(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  size_t total = 0;
+  for (int slot = 0; slot < WS_SLOTS; ++slot) total += g_ws_bytes[slot][dev];
+  return total;
+}
+
 int kmx_release_workspace(kmx_stream_t stream) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -823,6 +902,25 @@ int kmx_check_device_status(kmx_stream_t stream, int* flags) {
   }
   if (flags) *flags = host;
   return host ? KMX_ERR_DEVICE : KMX_OK;
+}
+
+int kmx_read_redo_counters(kmx_stream_t stream, unsigned long long* counts) {
+  unsigned long long* dp = nullptr;
+  int rc = redo_ptr(&dp);
+  if (rc != KMX_OK) return rc;
+  unsigned long long host[2] = {0, 0};
+  cudaError_t e =
+      cudaMemcpyAsync(host, dp, sizeof(host), cudaMemcpyDeviceToHost, KMX_STREAM(stream));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(KMX_STREAM(stream));
+  if (e != cudaSuccess) return cuda_fail(e);
+  e = cudaMemsetAsync(dp, 0, sizeof(host), KMX_STREAM(stream));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(KMX_STREAM(stream));
+  if (e != cudaSuccess) return cuda_fail(e);
+  if (counts) {
+    counts[0] = host[0];
+    counts[1] = host[1];
+  }
+  return KMX_OK;
 }
 
 int kmx_last_cuda_error(void) { return t_last_cuda_error; }

@@ -88,7 +88,55 @@ struct Problem {
   const long long* a_off;  // L_MIXED: first factor pointer of instance i in A
   const int* count_dev;    // when set, the entry count is read from device memory
   const int* order_base;   // when set, offset of this launch's entries in order[]
+  // diagnostic counters (may be null): [0] double-float entries recomputed in
+  // FP64 by the cancellation guard, [1] digits-form entries handed to the
+  // double-float pass
+  unsigned long long* redo_ctr;
+  int guard_off;         // nonzero: double-float without the cancellation guard
+  // test hook (set from the host environment, see run_problem): nonzero makes
+  // each group's first wait on a staged copy report that it ran out, so that
+  // the timeout path -- drain the copy, flag DF_WAIT_TIMEOUT, leave -- runs
+  // without a real stall
+  int wait_expire;
 };
+
+// ---------------------------------------------------------------------------
+// Cancellation guard of the double-float forms.
+//
+// Double-float carries about 48 bits, so its error on one entry is about
+// 2^-48 |K||X| (elementwise), where plain FP64's is about 2^-53 d n |K||X|:
+// when KX is much smaller than |K||X| (cancellation), the double-float result
+// loses accuracy first.  |K||X| is not available cheaply, but its norm is
+// bounded by prod_l ||A_l||_F ||X||_2, and for random (isotropic) data
+//     rho_F = ||KX||_2 sqrt(N) / (prod_l ||A_l||_F ||X||_2)
+// stays near 1 (above 0.2 for every shape at the 1e-4 quantile, measured on
+// Gaussian and uniform inputs), falling in proportion to the cancellation.
+// An entry with rho_F < 1/4 is recomputed in plain FP64: the double-float
+// error times rho_F stays below about 8e-14, so the entries it keeps are
+// within about 3e-13 even in the worst case measured and within 1e-13 on
+// every cancelling family tested.  The three norms are summed in FP32 from
+// the scaled high parts (the scale factors cancel in rho_F).
+// ---------------------------------------------------------------------------
+constexpr float GUARD_INV_TAU2 = 16.f;  // 1 / tau^2 with tau = 1/4
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// true when the entry must be recomputed in FP64: out2 = ||KX||^2, x2 = ||X||^2,
+// a2[l] = ||A_l||_F^2 (all of scaled values), N = length of X (for m_l x n_l
+// factors E||A v||^2 = ||A||_F^2 ||v||^2 / n_l, so prod n_l is the normaliser)
+__device__ __forceinline__ bool guard_fails(float out2, float x2, const float* a2, int d, long long N) {
+  float rhs = x2;
+  for (int l = 0; l < d; ++l) rhs *= a2[l];
+  return out2 * (float)N * GUARD_INV_TAU2 < rhs;
+}
+
+__device__ __forceinline__ void count_redo(const unsigned long long* ctr_base, int which) {
+  if (ctr_base) atomicAdd(const_cast<unsigned long long*>(ctr_base) + which, 1ull);
+}
 
 // Entries of a launch (device-side count when the host does not know it).
 __device__ __forceinline__ long long launch_count(const Problem& p) {
@@ -412,11 +460,62 @@ struct Rows {
 };
 
 // ---------------------------------------------------------------------------
+// Dot products of the plain kernels.  RD == false: fused multiply-add in T.
+// RD == true (FP32 data): every product exact as an FP32 pair, the pairs
+// summed with error-free two-sums and the sum rounded once to FP32 -- what
+// the reference's float kernels get by accumulating each dot product in
+// double and rounding it when stored (kgemm_nt.hpp:557-571,
+// kgemm_nn.hpp:688-701), to within about 2^-48 before that rounding.
+// ---------------------------------------------------------------------------
+template <typename T, bool RD>
+struct DotAcc {
+  T s;
+  __device__ __forceinline__ void first(T a, T v) { s = a * v; }
+  __device__ __forceinline__ void add(T a, T v) { s = fma(a, v, s); }
+  __device__ __forceinline__ T get() const { return s; }
+};
+template <>
+struct DotAcc<float, true> {
+  float s, c;
+  __device__ __forceinline__ void first(float a, float v) {
+    s = __fmul_rn(a, v);
+    c = __fmaf_rn(a, v, -s);
+  }
+  __device__ __forceinline__ void add(float a, float v) {
+    const float p = __fmul_rn(a, v);
+    const float e = __fmaf_rn(a, v, -p);
+    float t, te;
+    two_sum(s, p, t, te);
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(te, e));
+  }
+  __device__ __forceinline__ float get() const { return __fadd_rn(s, c); }
+};
+
+// sum_j a[j] * v[j*vs], j < NN
+template <typename T, bool RD, int NN>
+__device__ __forceinline__ T dot_n(const T* a, const T* v, long long vs = 1) {
+  DotAcc<T, RD> acc;
+  acc.first(a[0], v[0]);
+#pragma unroll
+  for (int j = 1; j < NN; ++j) acc.add(a[j], v[(long long)j * vs]);
+  return acc.get();
+}
+// run-time length nk
+template <typename T, bool RD>
+__device__ __forceinline__ T dot_rt(const T* a, const T* v, long long vs, int nk) {
+  DotAcc<T, RD> acc;
+  acc.first(a[0], v[0]);
+  for (int j = 1; j < nk; ++j) acc.add(a[j], v[(long long)j * vs]);
+  return acc.get();
+}
+
+// ---------------------------------------------------------------------------
 // Plain form, square factors, compile-time n = NN.
 // Shared memory per group: [d*NN*NN factor entries][N intermediates].
 // With GBUF the intermediate lives in a global workspace instead.
 // ---------------------------------------------------------------------------
-template <typename T, int NN, bool GBUF>
+template <typename T, int NN, bool GBUF, bool RD = false>
 __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs<T>& en, T* sA,
                                                T* buf, int lt, int G, int g) {
   constexpr int NN2 = NN * NN;
@@ -432,10 +531,10 @@ __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs
   const bool excl = p.y_exclusive != 0;
   if (d == 1) {
     for (int i = lt; i < NN; i += G) {
-      T acc = sA[i * NN] * __ldg(en.X);
+      T xv[NN];
 #pragma unroll
-      for (int j = 1; j < NN; ++j) acc = fma(sA[i * NN + j], __ldg(en.X + j), acc);
-      y_accumulate(en.Y + i, acc, excl);
+      for (int j = 0; j < NN; ++j) xv[j] = __ldg(en.X + j);
+      y_accumulate(en.Y + i, dot_n<T, RD, NN>(sA + i * NN, xv), excl);
     }
     return;
   }
@@ -448,13 +547,7 @@ __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs
 #pragma unroll
       for (int j = 0; j < NN; ++j) v[j] = __ldg(en.X + (long long)j * F + f);
 #pragma unroll
-      for (int r = 0; r < NN; ++r) {
-        const T* ar = a.row(r);
-        T acc = ar[0] * v[0];
-#pragma unroll
-        for (int j = 1; j < NN; ++j) acc = fma(ar[j], v[j], acc);
-        buf[(long long)r * F + f] = acc;
-      }
+      for (int r = 0; r < NN; ++r) buf[(long long)r * F + f] = dot_n<T, RD, NN>(a.row(r), v);
     }
   }
   group_sync(g, G);
@@ -472,13 +565,7 @@ __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs
 #pragma unroll
       for (int j = 0; j < NN; ++j) v[j] = base[(long long)j * s];
 #pragma unroll
-      for (int r = 0; r < NN; ++r) {
-        const T* ar = a.row(r);
-        T acc = ar[0] * v[0];
-#pragma unroll
-        for (int j = 1; j < NN; ++j) acc = fma(ar[j], v[j], acc);
-        base[(long long)r * s] = acc;
-      }
+      for (int r = 0; r < NN; ++r) base[(long long)r * s] = dot_n<T, RD, NN>(a.row(r), v);
     }
     group_sync(g, G);
   }
@@ -488,15 +575,12 @@ __device__ __forceinline__ void sq_plain_entry(const Problem& p, const EntryPtrs
     for (int i = lt; i < N; i += G) {
       const int f = i / NN, r = i - f * NN;
       const T* v = buf + (long long)f * NN;
-      T acc = Ad[r * NN] * v[0];
-#pragma unroll
-      for (int j = 1; j < NN; ++j) acc = fma(Ad[r * NN + j], v[j], acc);
-      y_accumulate(en.Y + i, acc, excl);
+      y_accumulate(en.Y + i, dot_n<T, RD, NN>(Ad + r * NN, v), excl);
     }
   }
 }
 
-template <typename T, int NN, bool GBUF>
+template <typename T, int NN, bool GBUF, bool RD = false>
 __global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int G = p.group_threads;
@@ -526,7 +610,7 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) 
         continue;
       }
     }
-    sq_plain_entry<T, NN, GBUF>(p, en, sA, buf, lt, G, g);
+    sq_plain_entry<T, NN, GBUF, RD>(p, en, sA, buf, lt, G, g);
     group_sync(g, G);
   }
 }
@@ -542,6 +626,12 @@ __global__ void __launch_bounds__(MAX_THREADS) sq_plain_kernel(const Problem p) 
 // otherwise takes); a minimum of 0 CTAs leaves the on-chip variants' register
 // choice to the compiler.
 // ---------------------------------------------------------------------------
+// Shared-memory head of the split per-mode kernels: d*NN*NN factor pairs,
+// MAXD+2 exponent ints, 2 x (MAXD+2) cancellation-guard sums.
+__host__ __device__ constexpr size_t sq_split_head(int nn) {
+  return ((size_t)MAXD * nn * nn * 8 + (MAXD + 2) * 4 + 2 * (MAXD + 2) * 4 + 15) / 16 * 16;
+}
+
 template <int NN, bool GBUF>
 __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_split_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -557,13 +647,14 @@ __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_spl
   unsigned char* gbase = smem + (size_t)g * p.group_smem;
   df* sA = reinterpret_cast<df*>(gbase);                        // d*NN2 pairs
   int* sExp = reinterpret_cast<int*>(gbase + MAXD * NN2 * sizeof(df));  // MAXD+2 ints
-  unsigned char* sbuf_raw =
-      gbase + ((MAXD * NN2 * sizeof(df) + (MAXD + 2) * sizeof(int) + 15) / 16 * 16);
+  float* sNrm0 = reinterpret_cast<float*>(sExp + MAXD + 2);     // [2][MAXD+2] guard sums
+  unsigned char* sbuf_raw = gbase + sq_split_head(NN);
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
   const bool excl = p.y_exclusive != 0;
   const long long count = launch_count(p);
   const long long obase = p.order_base ? (long long)*p.order_base : 0;
+  int par = 0;  // guard sums alternate between two slots (entry parity)
   for (long long e = slot0; e < count; e += step) {
     const long long entry = p.order ? (long long)p.order[obase + e] : e + p.entry_offset;
     EntryPtrs<double> en;
@@ -582,7 +673,12 @@ __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_spl
     }
     df* buf = reinterpret_cast<df*>(bufp);
     // --- scales: max exponent field per factor and of X ---
-    if (lt < MAXD + 2) sExp[lt] = 0;
+    float* sNrm = sNrm0 + par * (MAXD + 2);
+    par ^= 1;
+    if (lt < MAXD + 2) {
+      sExp[lt] = 0;
+      sNrm[lt] = 0.f;
+    }
     group_sync(g, G);
     {
       int emax[MAXD];
@@ -638,34 +734,70 @@ __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_spl
       const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
       const double* Al = en.A[l];
       const double v = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
-      sA[i] = split_scaled(v, sExp[l]);
+      const df s = split_scaled(v, sExp[l]);
+      sA[i] = s;
+      atomicAdd(&sNrm[l], s.hi * s.hi);
     }
     const int ex = sExp[MAXD];
     group_sync(g, G);
-    if (d == 1) {
-      for (int i = lt; i < NN; i += G) {
-        df v[NN];
+    float gsum = 0.f;  // guard: this thread's part of ||X||^2, then of ||KX||^2
+    // The last mode (d == 1: the only one), adding sign * its contribution to Y.
+    auto last_mode = [&](bool neg, bool norm) {
+      if (d == 1) {
+        for (int i = lt; i < NN; i += G) {
+          df v[NN];
 #pragma unroll
-        for (int j = 0; j < NN; ++j) v[j] = split_scaled(__ldg(en.X + j), ex);
-        const df o = df_dot<NN>(sA + i * NN, v);
+          for (int j = 0; j < NN; ++j) v[j] = split_scaled(__ldg(en.X + j), ex);
+          const df o = df_dot<NN>(sA + i * NN, v);
+          if (norm) gsum = __fmaf_rn(o.hi, o.hi, gsum);
+          const double y = f32_to_f64_scaled(o.hi, escale) + f32_to_f64_scaled(o.lo, escale);
+          y_accumulate(en.Y + i, neg ? -y : y, excl);
+        }
+        return;
+      }
+      const df* Ad = sA + (d - 1) * NN2;
+      for (int i = lt; i < N; i += G) {
+        const int f = i / NN, r = i - f * NN;
+        df v[NN], a[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          v[j] = buf[(long long)f * NN + j];
+          a[j] = Ad[r * NN + j];
+        }
+        const df o = df_dot<NN>(a, v);
+        if (norm) gsum = __fmaf_rn(o.hi, o.hi, gsum);
         const double y = f32_to_f64_scaled(o.hi, escale) + f32_to_f64_scaled(o.lo, escale);
-        y_accumulate(en.Y + i, y, excl);
+        y_accumulate(en.Y + i, neg ? -y : y, excl);
       }
-      group_sync(g, G);
-      continue;
-    }
-    // mode 0: X (HBM) -> buf
-    {
-      Rows<df, NN> a;
-      a.load(sA);
-      for (int f = lt; f < F; f += G) {
-        df v[NN];
+    };
+    if (d == 1) {
+      if (lt < NN) {
+        const df x = split_scaled(__ldg(en.X + lt), ex);
+        gsum = x.hi * x.hi;
+      }
+    } else {
+      // mode 0: X (HBM) -> buf
+      {
+        Rows<df, NN> a;
+        a.load(sA);
+        for (int f = lt; f < F; f += G) {
+          df v[NN];
 #pragma unroll
-        for (int j = 0; j < NN; ++j) v[j] = split_scaled(__ldg(en.X + (long long)j * F + f), ex);
+          for (int j = 0; j < NN; ++j) {
+            v[j] = split_scaled(__ldg(en.X + (long long)j * F + f), ex);
+            gsum = __fmaf_rn(v[j].hi, v[j].hi, gsum);
+          }
 #pragma unroll
-        for (int r = 0; r < NN; ++r) buf[(long long)r * F + f] = df_dot<NN>(a.row(r), v);
+          for (int r = 0; r < NN; ++r) buf[(long long)r * F + f] = df_dot<NN>(a.row(r), v);
+        }
       }
     }
+    gsum = warp_sum(gsum);
+    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD], gsum);
+    gsum = 0.f;
+    if (d == 1) {
+      last_mode(false, true);
+    } else {
     group_sync(g, G);
     int s = F / NN;
     for (int k = 1; k < d - 1; ++k, s /= NN) {
@@ -684,22 +816,22 @@ __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_spl
       }
       group_sync(g, G);
     }
-    {
-      const df* Ad = sA + (d - 1) * NN2;
-      for (int i = lt; i < N; i += G) {
-        const int f = i / NN, r = i - f * NN;
-        df v[NN], a[NN];
-#pragma unroll
-        for (int j = 0; j < NN; ++j) {
-          v[j] = buf[(long long)f * NN + j];
-          a[j] = Ad[r * NN + j];
-        }
-        const df o = df_dot<NN>(a, v);
-        const double y = f32_to_f64_scaled(o.hi, escale) + f32_to_f64_scaled(o.lo, escale);
-        y_accumulate(en.Y + i, y, excl);
-      }
+    last_mode(false, true);
     }
+    gsum = warp_sum(gsum);
+    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD + 1], gsum);
     group_sync(g, G);
+    // cancellation guard (uniform over the group): take the contribution back
+    // (the intermediate is unchanged, the same arithmetic gives the same
+    // values) and add the plain FP64 result instead
+    if (!p.guard_off && guard_fails(sNrm[MAXD + 1], sNrm[MAXD], sNrm, d, N)) {
+      last_mode(true, false);
+      group_sync(g, G);
+      sq_plain_entry<double, NN, GBUF>(p, en, reinterpret_cast<double*>(gbase),
+                                       reinterpret_cast<double*>(bufp), lt, G, g);
+      if (lt == 0) count_redo(p.redo_ctr, 0);
+      group_sync(g, G);
+    }
   }
 }
 
@@ -715,7 +847,7 @@ constexpr int GEN_MAXN = 64;
 
 // One entry of the generic plain kernel (also the Inf/NaN fallback of the
 // generic split kernel): factors into sA, modes through b0/b1, Y += result.
-template <typename T>
+template <typename T, bool RD = false>
 __device__ __forceinline__ void gen_plain_entry(const Problem& p, const EntryPtrs<T>& en, T* sA,
                                                 T* b0, T* b1, int lt, int G, int g) {
   const int d = p.d;
@@ -752,11 +884,7 @@ __device__ __forceinline__ void gen_plain_entry(const Problem& p, const EntryPtr
         T* base = cur + (long long)o * nk * s + r0;
         T v[GEN_MAXN];
         for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
-        for (int a = 0; a < mk; ++a) {
-          T acc = Ak[a * nk] * v[0];
-          for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[j], acc);
-          base[(long long)a * s] = acc;
-        }
+        for (int a = 0; a < mk; ++a) base[(long long)a * s] = dot_rt<T, RD>(Ak + a * nk, v, 1, nk);
       }
     } else {
       // out of place: one output element per lane
@@ -769,8 +897,7 @@ __device__ __forceinline__ void gen_plain_entry(const Problem& p, const EntryPtr
         const unsigned o = fm(t);
         const int a = (int)(t - o * (unsigned)mk);
         const T* v = src + (long long)o * nk * s + rr;
-        T acc = Ak[a * nk] * v[0];
-        for (int j = 1; j < nk; ++j) acc = fma(Ak[a * nk + j], v[(long long)j * s], acc);
+        const T acc = dot_rt<T, RD>(Ak + a * nk, v, s, nk);
         if (last) {
           y_accumulate(dst + q, acc, excl);
         } else {
@@ -785,7 +912,7 @@ __device__ __forceinline__ void gen_plain_entry(const Problem& p, const EntryPtr
   }
 }
 
-template <typename T, bool GBUF>
+template <typename T, bool GBUF, bool RD = false>
 __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int G = p.group_threads;
@@ -816,7 +943,7 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
         continue;
       }
     }
-    gen_plain_entry<T>(p, en, sA, b0, b1, lt, G, g);
+    gen_plain_entry<T, RD>(p, en, sA, b0, b1, lt, G, g);
   }
 }
 
@@ -833,10 +960,12 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_plain_kernel(const Problem p)
 // but the last are all square with n <= GEN_SPLIT_MAXN) those modes run in
 // place, the lane holding its fiber.  The last mode widens to FP64 and adds
 // to Y.  Entries with Inf/NaN run the plain entry.
-// Shared memory per group: [factors as pairs][MAXD+2 exponents, 64 bytes]
-// [sxw pairs][sxw pairs when two buffers] (buffers in the workspace with GBUF).
+// Shared memory per group: [factors as pairs][MAXD+2 exponents, 2 x (MAXD+2)
+// guard sums: GEN_SPLIT_HDR bytes][sxw pairs][sxw pairs when two buffers]
+// (buffers in the workspace with GBUF).
 // ---------------------------------------------------------------------------
 constexpr int GEN_SPLIT_MAXN = 16;
+constexpr int GEN_SPLIT_HDR = 128;
 
 // A mode the generic split kernel can apply in place.
 __host__ __device__ inline bool gen_split_in_place(int m, int n) {
@@ -893,14 +1022,16 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
   unsigned char* gbase = smem + (size_t)g * p.group_smem;
   df* sA = reinterpret_cast<df*>(gbase);
   const size_t fac_bytes = ((size_t)aoff[d] * 8 + 15) / 16 * 16;
-  int* sExp = reinterpret_cast<int*>(gbase + fac_bytes);  // MAXD + 2 ints (64 bytes)
-  unsigned char* braw = gbase + fac_bytes + 64;
+  int* sExp = reinterpret_cast<int*>(gbase + fac_bytes);  // MAXD + 2 ints
+  float* sNrm0 = reinterpret_cast<float*>(sExp + MAXD + 2);  // [2][MAXD + 2] guard sums
+  unsigned char* braw = gbase + fac_bytes + GEN_SPLIT_HDR;
   const size_t bbytes = ((size_t)p.sxw * 8 + 15) / 16 * 16;
-  const bool two = GBUF || (size_t)p.group_smem >= fac_bytes + 64 + 2 * bbytes;
+  const bool two = GBUF || (size_t)p.group_smem >= fac_bytes + GEN_SPLIT_HDR + 2 * bbytes;
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
   const bool excl = p.y_exclusive != 0;
   const long long Nx = p.Nx;
+  int par = 0;  // guard sums alternate between two slots (entry parity)
   EntryStream es(p, slot0, step);
   for (long long entry; es.next(p, entry);) {
     EntryPtrs<double> en;
@@ -908,6 +1039,8 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
       if (lt == 0) atomicOr(p.status, DF_NULL_PTR);
       continue;
     }
+    float* sNrm = sNrm0 + par * (MAXD + 2);
+    par ^= 1;
     double *w0 = reinterpret_cast<double*>(braw), *w1 = reinterpret_cast<double*>(braw + bbytes);
     if (GBUF) {
       if (!workspace<double>(p, entry, slot0, w0, w1)) {
@@ -916,7 +1049,10 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
       }
     }
     // --- scales: max exponent field per factor and of X ---
-    if (lt < MAXD + 2) sExp[lt] = 0;
+    if (lt < MAXD + 2) {
+      sExp[lt] = 0;
+      sNrm[lt] = 0.f;
+    }
     group_sync(g, G);
     for (int l = 0; l < d; ++l) {
       const int ml = p.m[l], nl = p.n[l];
@@ -958,20 +1094,76 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
     // --- factors (transposed: sA[aoff[l] + j*m_l + a] = A_l(a, j)) and X, split ---
     for (int l = 0; l < d; ++l) {
       const int ml = p.m[l], nl = p.n[l];
+      float an = 0.f;
       for (int i = lt; i < ml * nl; i += G) {
         const int j = i / ml, a = i - j * ml;
-        sA[aoff[l] + i] = split_scaled(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
-                                               : en.A[l][a + (long long)j * en.ld[l]],
-                                       sExp[l]);
+        const df s = split_scaled(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                          : en.A[l][a + (long long)j * en.ld[l]],
+                                  sExp[l]);
+        sA[aoff[l] + i] = s;
+        an = __fmaf_rn(s.hi, s.hi, an);
       }
+      an = warp_sum(an);
+      if ((lt & 31) == 0) atomicAdd(&sNrm[l], an);
     }
     df* b0 = reinterpret_cast<df*>(w0);
     df* b1 = reinterpret_cast<df*>(w1);
     const int ex = sExp[MAXD];
-    for (long long i = lt; i < Nx; i += G) b0[i] = split_scaled(__ldg(en.X + i), ex);
+    float gsum = 0.f;  // guard: this thread's part of ||X||^2, then of ||KX||^2
+    for (long long i = lt; i < Nx; i += G) {
+      const df s = split_scaled(__ldg(en.X + i), ex);
+      b0[i] = s;
+      gsum = __fmaf_rn(s.hi, s.hi, gsum);
+    }
+    gsum = warp_sum(gsum);
+    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD], gsum);
+    gsum = 0.f;
     group_sync(g, G);
+    // Out of place: a lane owns rows a0..a0+R-1 of one fiber of mode k.  The
+    // last mode (dst == nullptr) adds its outputs to Y, or subtracts them (neg).
+    auto out_of_place = [&](int k, unsigned outer, const df* src, df* dst, bool neg) {
+      unsigned s = 1;
+      for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
+      const int mk = p.m[k], nk = p.n[k];
+      const df* At = sA + aoff[k];
+      const int nb = (mk + R - 1) / R;
+      const FastDiv fs(s), fb((unsigned)nb);
+      const unsigned total = outer * (unsigned)nb * s;
+      for (unsigned q = lt; q < total; q += G) {
+        const unsigned t = fs(q);
+        const unsigned rr = q - t * s;
+        const unsigned o = fb(t);
+        const int a0 = (int)(t - o * (unsigned)nb) * R;
+        const df* v = src + (long long)o * nk * s + rr;
+        df av[R];
+        DfRows<R> acc;
+#pragma unroll
+        for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
+        acc.first(av, v[0]);
+        for (int j = 1; j < nk; ++j) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
+          acc.add(av, v[(long long)j * s]);
+        }
+        const long long obase_q = ((long long)o * mk + a0) * s + rr;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (a0 + r < mk) {
+            const df o2 = acc.get(r);
+            if (dst == nullptr) {
+              if (!neg) gsum = __fmaf_rn(o2.hi, o2.hi, gsum);
+              const double y =
+                  f32_to_f64_scaled(o2.hi, escale) + f32_to_f64_scaled(o2.lo, escale);
+              y_accumulate(en.Y + obase_q + (long long)r * s, neg ? -y : y, excl);
+            } else {
+              dst[obase_q + (long long)r * s] = o2;
+            }
+          }
+        }
+      }
+    };
     df* cur = b0;
-    unsigned outer = 1;
+    unsigned outer = 1, outer_last = 1;
     for (int k = 0; k < d; ++k) {
       unsigned s = 1;
       for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
@@ -1007,45 +1199,25 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
           }
         }
       } else {
-        // out of place: a lane owns rows a0..a0+R-1 of one fiber
         df* dst = last ? nullptr : (cur == b0 ? b1 : b0);
-        const FastDiv fs(s), fb((unsigned)nb);
-        const unsigned total = outer * (unsigned)nb * s;
-        for (unsigned q = lt; q < total; q += G) {
-          const unsigned t = fs(q);
-          const unsigned rr = q - t * s;
-          const unsigned o = fb(t);
-          const int a0 = (int)(t - o * (unsigned)nb) * R;
-          const df* v = cur + (long long)o * nk * s + rr;
-          df av[R];
-          DfRows<R> acc;
-#pragma unroll
-          for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
-          acc.first(av, v[0]);
-          for (int j = 1; j < nk; ++j) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
-            acc.add(av, v[(long long)j * s]);
-          }
-          const long long obase_q = ((long long)o * mk + a0) * s + rr;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            if (a0 + r < mk) {
-              const df o2 = acc.get(r);
-              if (last) {
-                const double y =
-                    f32_to_f64_scaled(o2.hi, escale) + f32_to_f64_scaled(o2.lo, escale);
-                y_accumulate(en.Y + obase_q + (long long)r * s, y, excl);
-              } else {
-                dst[obase_q + (long long)r * s] = o2;
-              }
-            }
-          }
-        }
+        if (last) outer_last = outer;
+        out_of_place(k, outer, cur, dst, false);
         if (!last) cur = dst;
       }
       group_sync(g, G);
       outer *= (unsigned)mk;
+    }
+    gsum = warp_sum(gsum);
+    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD + 1], gsum);
+    group_sync(g, G);
+    // cancellation guard (uniform over the group): take the contribution back
+    // (the last mode leaves its input unchanged, the same arithmetic gives the
+    // same values) and add the plain FP64 result instead
+    if (!p.guard_off && guard_fails(sNrm[MAXD + 1], sNrm[MAXD], sNrm, d, Nx)) {
+      out_of_place(d - 1, outer_last, cur, nullptr, true);
+      group_sync(g, G);
+      gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
+      if (lt == 0) count_redo(p.redo_ctr, 0);
     }
   }
 }

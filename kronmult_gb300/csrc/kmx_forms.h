@@ -8,6 +8,15 @@ struct LaunchHint;
 cudaError_t launch_f64_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f64_split(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
+// Whether the FP64 forward of p needs a global workspace (an entry beyond
+// shared memory), decided as the launchers decide (seg: deterministic mode).
+bool needs_workspace_f64_plain(const Problem& p, bool seg, int engine);
+bool needs_workspace_f64_split(const Problem& p, bool seg, int engine);
+// The xbatched FP64 problem the C ABI would run for (d, n, lda) and the form
+// it would pick for `form` (KMX_FORM_*); KMX_OK or a kmx_status.
+int xbatched_f64_plan(int d, int n, int lda, int form, int accumulate, bool* needs_ws);
+// FP32 data, dot products rounded once (the reference's float kernels)
+cudaError_t launch_f32_ref(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_f32(Problem& p, const LaunchHint& h, cudaStream_t s);
 cudaError_t launch_wide_bf16(Problem& p, const LaunchHint& h, cudaStream_t s);
 // FP64 digits form on the FP16 tensor cores: redo (p.count ints) and

@@ -12,7 +12,10 @@
 
 namespace kmx {
 
-enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2, FORM_WIDE = 3 };
+// FORM_REF32: FP32 data, each dot product rounded once (the reference's float
+// semantics), per-mode kernels only (they apply the modes in the reference's
+// order, A1 first, rounding each stage to FP32 as it does).
+enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2, FORM_WIDE = 3, FORM_REF32 = 4 };
 
 // Execution shape requested by the caller (0 = choose).
 struct LaunchHint {
@@ -57,6 +60,8 @@ template <typename T, int FORM, int NN, bool GB>
 const void* sq_kernel() {
   if constexpr (FORM == FORM_SPLIT) {
     return reinterpret_cast<const void*>(&sq_split_kernel<NN, GB>);
+  } else if constexpr (FORM == FORM_REF32) {
+    return reinterpret_cast<const void*>(&sq_plain_kernel<T, NN, GB, true>);
   } else {
     return reinterpret_cast<const void*>(&sq_plain_kernel<T, NN, GB>);
   }
@@ -175,8 +180,7 @@ inline cudaError_t launch_tile(Problem& p, const TileKernel& k, const LaunchHint
 template <typename T, int FORM>
 size_t sq_group_smem(const Problem& p, bool gbuf) {
   const int nn = p.n[0];
-  size_t head = (FORM == FORM_SPLIT) ? align16(MAXD * nn * nn * 8 + (MAXD + 2) * sizeof(int))
-                                     : align16(MAXD * nn * nn * sizeof(T));
+  size_t head = (FORM == FORM_SPLIT) ? sq_split_head(nn) : align16(MAXD * nn * nn * sizeof(T));
   size_t buf = (p.d >= 2 && !gbuf) ? align16((size_t)p.Nx * (FORM == FORM_SPLIT ? 8 : sizeof(T))) : 0;
   return head + buf;
 }
@@ -199,18 +203,48 @@ size_t gen_group_smem(const Problem& p, bool gbuf) {
 // buffers.
 inline bool gen_split_wide(const Problem& p) { return p.Nx >= 4096 || p.Ny >= 4096; }
 
-// [factors as pairs][MAXD+2 exponents, 64 bytes][one or two buffers].  X
-// itself is split into the first buffer, so d = 1 needs one too.
+// [factors as pairs][exponents and guard sums, GEN_SPLIT_HDR bytes][one or
+// two buffers].  X itself is split into the first buffer, so d = 1 needs one too.
 inline size_t gen_split_group_smem(const Problem& p, bool gbuf, size_t limit) {
   size_t fac = 0;
   for (int l = 0; l < p.d; ++l) fac += (size_t)p.m[l] * p.n[l];
-  const size_t head = align16(fac * 8) + 64;
+  const size_t head = align16(fac * 8) + GEN_SPLIT_HDR;
   if (gbuf) return head;
   const size_t b = align16((size_t)p.sxw * 8);
   bool one_ok = true;
   for (int k = 0; k + 1 < p.d; ++k) one_ok = one_ok && gen_split_in_place(p.m[k], p.n[k]);
   if (one_ok && (gen_split_wide(p) || head + 2 * b > limit)) return head + b;
   return head + 2 * b;
+}
+
+// Whether launch_forward would need a global workspace for p (an entry too
+// large for shared memory), decided as it decides, without launching.  seg:
+// the deterministic (segment) mode; engine: the LaunchHint engine.
+template <typename T, int FORM>
+bool needs_workspace(const Problem& p, bool seg, int engine) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return true;
+  const DeviceInfo di = device_info(dev);
+  const bool square = is_square(p);
+  const int nn = p.n[0];
+  if constexpr (FORM != FORM_REF32) {
+    if (seg && square && !p.seg_key && pick_tile<T, FORM, true>(nn, p.d).func) return false;
+    if (!seg && square && engine != 1 && pick_tile<T, FORM>(nn, p.d).func) return false;
+  }
+  if constexpr (FORM == FORM_WIDE) {
+    return false;
+  } else {
+    const bool spec = !seg && square && pick_sq<T, FORM, false>(nn) != nullptr;
+    size_t gsm;
+    if (spec) {
+      gsm = sq_group_smem<T, FORM>(p, false);
+    } else if constexpr (FORM == FORM_SPLIT) {
+      gsm = gen_split_group_smem(p, false, di.max_smem_optin);
+    } else {
+      gsm = gen_group_smem<T>(p, false);
+    }
+    return gsm > (size_t)di.max_smem_optin;
+  }
 }
 
 // Launch one forward pass over p.count entries.  Returns cudaSuccess, or the
@@ -226,16 +260,18 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   const bool square = is_square(p);
   const int nn = p.n[0];
   const bool seg = p.seg_entries != nullptr;
-  if (seg) {
-    // deterministic mode: the register-tiled segment kernels where they
-    // exist, else the generic kernels walking whole segments (EntryStream)
-    // (class-filtered segments of mixed-shape calls: generic kernels only)
-    const TileKernel tk = square && !p.seg_key ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
-    if (tk.func) return launch_tile(p, tk, hint, stream);
-  }
-  if (!seg && square && hint.engine != 1) {
-    const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
-    if (tk.func) return launch_tile(p, tk, hint, stream);
+  if constexpr (FORM != FORM_REF32) {
+    if (seg) {
+      // deterministic mode: the register-tiled segment kernels where they
+      // exist, else the generic kernels walking whole segments (EntryStream)
+      // (class-filtered segments of mixed-shape calls: generic kernels only)
+      const TileKernel tk = square && !p.seg_key ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
+      if (tk.func) return launch_tile(p, tk, hint, stream);
+    }
+    if (!seg && square && hint.engine != 1) {
+      const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
+      if (tk.func) return launch_tile(p, tk, hint, stream);
+    }
   }
   if constexpr (FORM == FORM_WIDE) {
     return cudaErrorNotSupported;  // register-tiled shapes only (handled above)
@@ -265,6 +301,9 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
       func = gbuf ? reinterpret_cast<const void*>(&gen_split_kernel<true, 2>)
                   : reinterpret_cast<const void*>(&gen_split_kernel<false, 2>);
     }
+  } else if constexpr (FORM == FORM_REF32) {
+    func = gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true, true>)
+                : reinterpret_cast<const void*>(&gen_plain_kernel<T, false, true>);
   } else {
     func = gbuf ? reinterpret_cast<const void*>(&gen_plain_kernel<T, true>)
                 : reinterpret_cast<const void*>(&gen_plain_kernel<T, false>);

@@ -14,9 +14,16 @@
 //   - Capacity: KMX_NOALLOC_SCRATCH_BYTES (16 MiB) per GPU, held from module
 //     load until process exit; calls whose scratch would exceed it are
 //     rejected with KMX_ERR_WORKSPACE before anything is launched.
+//   - Shapes: every square shape whose entry fits in on-chip memory; an entry
+//     that would need a global workspace for its intermediate (n = 8 with
+//     d >= 5, for example) is rejected with KMX_ERR_UNSUPPORTED, also before
+//     anything is launched.
 //   - Set-up: the first call on a device, with that device current, looks up
-//     the array's device address with cudaGetSymbolAddress and caches it.
-//     Make that first call before any stream capture begins.
+//     the array's device address with cudaGetSymbolAddress and caches it for
+//     the life of the process.  Make that first call before any stream
+//     capture begins.  The cached address belongs to the device's primary
+//     context: after cudaDeviceReset it is stale, so do not use the library
+//     across a device reset.
 //   - Sharing: every call uses the same array and the array keeps the last
 //     call's contents; each call zeroes what must start at zero (segment
 //     counts, the work-queue counter) on its stream.  Calls that overlap on
@@ -26,6 +33,7 @@
 #include <mutex>
 
 #include "../../include/kronmult_gb300.h"
+#include "kmx_forms.h"
 #include "kmx_segments.h"
 
 namespace {
@@ -61,10 +69,15 @@ extern "C" int kmx_kronmult_xbatched_f64_noalloc(int d, int n, const double* con
                                                  double* const* pX, double* const* pY,
                                                  int batchCount, kmx_stream_t stream) {
   if (batchCount < 0) return KMX_ERR_INVALID_ARG;
+  // shape and argument checks, then capacity, all before anything is launched
+  bool needs_ws = false;
+  int rc = kmx::xbatched_f64_plan(d, n, lda, KMX_FORM_AUTO, KMX_ACC_DETERMINISTIC, &needs_ws);
+  if (rc != KMX_OK) return rc;
+  if (needs_ws) return KMX_ERR_UNSUPPORTED;
   if (batchCount == 0) return KMX_OK;
   if (kmx::seg_workspace_bytes(batchCount) > KMX_NOALLOC_SCRATCH_BYTES) return KMX_ERR_WORKSPACE;
   void* scratch = nullptr;
-  const int rc = noalloc_scratch(&scratch);
+  rc = noalloc_scratch(&scratch);
   if (rc != KMX_OK) return rc;
   kmx_options o;
   o.form = KMX_FORM_AUTO;

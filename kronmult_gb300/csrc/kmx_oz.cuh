@@ -81,6 +81,8 @@ struct Smem {
   int emax;                    // X block: largest biased exponent
   int flags;                   // OZ_* bits of the entry
   int top[P];                  // per step: bit 0 a digit at position 0, bit 1 at position 1
+  float gn[P + 2];             // cancellation guard: ||F_ph||^2 (2^(ef-1021) units), ||X||^2
+                               // (2^(emax-1023) units), ||KX||^2 (2^es units)
 };
 
 // |x| as a 63-bit fraction of 2^E (E = emax - 1022): digit s (0..6) is bits
@@ -286,12 +288,34 @@ __device__ __forceinline__ void steps(Smem<NN, D>& S, const double (&xv)[Shape<N
     steps<NN, D, PH + 1>(S, xv, ntop, E + efs + 9 * (1 - ntop), warp, g, t, yp);
   } else {
     if (__any_sync(0xffffffffu, big) && (threadIdx.x & 31) == 0) atomicOr(&S.flags, OZ_BIG);
+    float o2 = 0.f;
+#pragma unroll
+    for (int j = 0; j < SH::TPW; ++j) {
+      if (warp + j * WARPS >= SH::NT) break;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o2 = __fmaf_rn(ov[j][q][0], ov[j][q][0], o2);
+    }
+    o2 = warp_sum(o2);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&S.gn[SH::P + 1], o2);
     __syncthreads();
-    if (!(S.flags & OZ_BIG)) {
+    const int es = E + efs;
+    // cancellation guard of the double-float forms (kmx_engine.cuh), with the
+    // three norms brought to one scale: the output carries 2^es, X 2^(emax-1023),
+    // factor F_ph 2^(ef_ph-1021)
+    int delta = es - (S.emax - 1023);
+#pragma unroll
+    for (int ph = 0; ph < SH::P; ++ph) delta -= S.ef[ph] - 1021;
+    float rhs = S.gn[SH::P];
+#pragma unroll
+    for (int ph = 0; ph < SH::P; ++ph) rhs *= S.gn[ph];
+    const bool cancel =
+        delta < 0 || delta > 60 ||
+        S.gn[SH::P + 1] * __int_as_float((127 + 2 * delta) << 23) * (float)SH::N * GUARD_INV_TAU2 <
+            rhs;
+    if (!(S.flags & OZ_BIG) || cancel) {
       if (threadIdx.x == 0) atomicOr(&S.flags, OZ_REDO);
       return;
     }
-    const int es = E + efs;
 #pragma unroll
     for (int j = 0; j < SH::TPW; ++j) {
       const int nt = warp + j * WARPS;
@@ -325,6 +349,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
       S.ef[threadIdx.x] = 0;
       S.top[threadIdx.x] = 0;
     }
+    if (threadIdx.x < SH::P + 2) S.gn[threadIdx.x] = 0.f;
     if (threadIdx.x == 0) {
       S.flags = 0;
       S.emax = 0;
@@ -368,6 +393,19 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
     }
     xe = __reduce_max_sync(0xffffffffu, xe);
     if (lane == 0) atomicMax(&S.emax, xe);
+    __syncthreads();  // block exponent of X final (for the guard's norm of X)
+    {
+      float x2 = 0.f;
+#pragma unroll
+      for (int j = 0; j < SH::TPW; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float h = split_scaled(xv[j][q], S.emax).hi;
+          x2 = __fmaf_rn(h, h, x2);
+        }
+      x2 = warp_sum(x2);
+      if (lane == 0) atomicAdd(&S.gn[SH::P], x2);
+    }
     // combined factors of every step; their block exponents
     for (int idx = threadIdx.x; idx < SH::P * 256; idx += THREADS) {
       const int ph = idx >> 8, i = (idx >> 4) & 15, k = idx & 15;
@@ -389,7 +427,10 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
       if (S.ef[ph] == 2047 && threadIdx.x == 0) atomicOr(&S.flags, OZ_REDO);
     __syncthreads();
     if (S.flags & OZ_REDO) {
-      if (threadIdx.x == 0) redo[atomicAdd(redo_count, 1)] = (int)ent;
+      if (threadIdx.x == 0) {
+        redo[atomicAdd(redo_count, 1)] = (int)ent;
+        count_redo(p.redo_ctr, 1);
+      }
       continue;
     }
     if (skip) continue;
@@ -403,6 +444,8 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
         f = S.a[ph][i][k];
       }
       df u = split_scaled(f, S.ef[ph] + 2);
+      const float fn = warp_sum(u.hi * u.hi);  // a warp's 32 elements share ph
+      if ((threadIdx.x & 31) == 0) atomicAdd(&S.gn[ph], fn);
       float hi = u.hi, lo = u.lo;
 #pragma unroll
       for (int sd = 0; sd < NP; ++sd) {
@@ -417,7 +460,10 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const Problem p, int* re
     __syncthreads();
     steps<NN, D, 0>(S, xv, 0, S.emax - 1022, warp, g, t, yp);
     __syncthreads();
-    if ((S.flags & OZ_REDO) && threadIdx.x == 0) redo[atomicAdd(redo_count, 1)] = (int)ent;
+    if ((S.flags & OZ_REDO) && threadIdx.x == 0) {
+      redo[atomicAdd(redo_count, 1)] = (int)ent;
+      count_redo(p.redo_ctr, 1);
+    }
   }
 }
 

@@ -363,6 +363,7 @@ __device__ __forceinline__ const T* a_ptr(const Problem& p, long long ent, int l
 //   [d*NN*NN factor entries of V]
 //   [2 x (MAXD+1) exponent ints][2 flag ints][stage-mode int][pad]   (by entry parity)
 //   [2 entry descriptors (long long id, int flags, pad)]
+//   [2 x (MAXD+2) cancellation-guard sums (float)]                    (by entry parity)
 //   [mbarrier]
 //   [X staging block: N x In]
 //   [intermediate: buffer_slots x V]
@@ -376,9 +377,15 @@ template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_desc() {
   return (off_ints<Pol, NN, D>() + (2 * (MAXD + 1) + 4) * 4 + 15) / 16 * 16;
 }
+// cancellation-guard sums, by entry parity: ||A_l||^2 (l < MAXD), ||X||^2, ||KX||^2
+template <class Pol, int NN, int D>
+__host__ __device__ constexpr int off_nrm() {
+  return off_desc<Pol, NN, D>() + 2 * 16;
+}
+constexpr int NRM_STRIDE = MAXD + 2;
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_bars() {
-  return off_desc<Pol, NN, D>() + 2 * 16;
+  return off_nrm<Pol, NN, D>() + 2 * NRM_STRIDE * 4;
 }
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_stage() {
@@ -427,6 +434,52 @@ __device__ __noinline__ void nonfinite_entry(const Problem& p, long long ent, do
   EntryPtrs<double> en;
   resolve_entry<double>(p, ent, en);
   sq_plain_entry<double, NN, false>(p, en, sA, buf, lt, G, g);
+}
+
+// The cancellation guard fired for this entry (double-float policy only): take
+// back what the last phase added -- recomputed from the intermediate, which the
+// last phase leaves unchanged, by the same arithmetic, so bitwise the same
+// values -- and add the plain FP64 result instead.  Out of line: rarely taken.
+template <class Pol, int NN, int D, bool SEG>
+__device__ __noinline__ void guard_redo(const Problem& p, long long ent, typename Pol::V* sA,
+                                        typename Pol::V* buf, typename Pol::Out* acc,
+                                        typename Pol::Out* yp, int escale, bool last, int lt,
+                                        int g) {
+  using V = typename Pol::V;
+  using Out = typename Pol::Out;
+  constexpr int G = group_threads(NN, D);
+  constexpr int NN2 = NN * NN;
+  constexpr int LP = num_phases(NN, D) - 1;
+  constexpr int TL = tile_size(NN, D, LP);
+  constexpr int NTL = ipow(NN, D) / TL;
+  constexpr bool PAIRL = phase_b(NN, D, LP) >= 0;
+  constexpr int aL = phase_a(NN, D, LP);
+  constexpr int bL = PAIRL ? phase_b(NN, D, LP) : aL;
+  for (int u = lt; u < NTL; u += G) {
+    const int base = tile_base<NN, D, LP>(u);
+    V v[TL];
+#pragma unroll
+    for (int t = 0; t < TL; ++t) v[t] = buf[slot<NN>(base + tile_off<NN, D, LP>(t))];
+    contract_tile<Pol, NN, PAIRL>(v, sA + aL * NN2, sA + bL * NN2);
+#pragma unroll
+    for (int t = 0; t < TL; ++t) {
+      const int q = base + tile_off<NN, D, LP>(t);
+      const Out y = Pol::finish(v[t], escale);
+      if constexpr (SEG) {
+        if (last) {
+          yp[q] -= y;
+        } else {
+          acc[q] -= y;
+        }
+      } else {
+        atomicAdd(yp + q, -y);
+      }
+    }
+  }
+  group_sync(g, G);  // factors and intermediate free for the FP64 evaluation
+  nonfinite_entry<NN>(p, ent, reinterpret_cast<double*>(sA), reinterpret_cast<double*>(buf), lt,
+                      G, g);
+  if (lt == 0) count_redo(p.redo_ctr, 0);
 }
 
 enum : int { TF_NULL = 1, TF_TIMEOUT = 2 };
@@ -492,6 +545,7 @@ tile_kernel(const Problem p) {
   int* sFlag = sExp + 2 * (MAXD + 1);                                 // [2]
   int* sMode = sFlag + 2;                                             // [1]
   EntryDesc* sDesc = reinterpret_cast<EntryDesc*>(gb + off_desc<Pol, NN, D>());  // [2]
+  float* sNrm = reinterpret_cast<float*>(gb + off_nrm<Pol, NN, D>());  // [2][NRM_STRIDE]
   uint64_t* bar = reinterpret_cast<uint64_t*>(gb + off_bars<Pol, NN, D>());
   In* stage = reinterpret_cast<In*>(gb + off_stage<Pol, NN, D>());
   V* buf = reinterpret_cast<V*>(gb + off_buf<Pol, NN, D>());
@@ -526,6 +580,7 @@ tile_kernel(const Problem p) {
   };
 
   if (lt < 2 * (MAXD + 1) + 4) sExp[lt] = 0;
+  if (lt < 2 * NRM_STRIDE) sNrm[lt] = 0.f;
   if (lt == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
@@ -590,6 +645,8 @@ tile_kernel(const Problem p) {
     if (!(dk.flags & ED_VALID)) break;
     int* ex_k = sExp + pb * (MAXD + 1);
     int* ex_n = sExp + (pb ^ 1) * (MAXD + 1);
+    float* nrm_k = sNrm + pb * NRM_STRIDE;
+    float* nrm_n = sNrm + (pb ^ 1) * NRM_STRIDE;
     const long long ent = dk.ent;
     Out* yp = y_ptr<Out>(p, ent);
     const In* xnext = nullptr;
@@ -600,19 +657,32 @@ tile_kernel(const Problem p) {
       if (dn.flags & ED_VALID) xnext = x_ptr<In>(p, dn.ent);
     }
 #pragma unroll
-    for (int f = 0; f < FPT; ++f)
-      if (fthr[f]) sA[lt + f * G] = Pol::make(af[f], Pol::SCALED ? ex_k[al[f]] : 0);
+    for (int f = 0; f < FPT; ++f) {
+      if (fthr[f]) {
+        const V a = Pol::make(af[f], Pol::SCALED ? ex_k[al[f]] : 0);
+        sA[lt + f * G] = a;
+        if constexpr (Pol::SCALED) atomicAdd(&nrm_k[al[f]], a.hi * a.hi);
+      }
+    }
     if (lt <= MAXD) ex_n[lt] = 0;
     if (lt == 0) {
       sFlag[pb ^ 1] = 0;
       if (sMode[0]) {
-        const bool ok = mbar_wait(bar, uses & 1);
+        const bool ok = (p.wait_expire && uses == 0) ? false : mbar_wait(bar, uses & 1);
+        if (!ok) {
+          atomicOr(&sFlag[pb], TF_TIMEOUT);
+          // The bulk copy may still be writing the staging block: wait for it
+          // once more under the same bound, so that the group never leaves
+          // with a copy into shared memory in flight.
+          mbar_wait(bar, uses & 1);
+        }
         ++uses;
-        if (!ok) atomicOr(&sFlag[pb], TF_TIMEOUT);
       }
       if (!yp || !x_ptr<In>(p, ent)) atomicOr(&sFlag[pb], TF_NULL);
     }
     group_sync(g, G);  // S1: X staged, factors in shared memory, next descriptor published
+    // the other parity's guard sums: entry k-1 has been decided, k+1 starts later
+    if (Pol::SCALED && lt < NRM_STRIDE) nrm_n[lt] = 0.f;
     const int flags = sFlag[pb];
     if (flags & TF_TIMEOUT) {
       if (lt == 0) atomicOr(p.status, DF_WAIT_TIMEOUT);
@@ -735,11 +805,15 @@ tile_kernel(const Problem p) {
     }
 
     // ---- phase 0: registers -> buf ----
+    float gsum = 0.f;  // guard: this thread's part of ||X||^2, then of ||KX||^2
     if constexpr (ONE) {
       if (lt < NT0) {
         V v[T0];
 #pragma unroll
-        for (int t = 0; t < T0; ++t) v[t] = Pol::make(xv[t], ex);
+        for (int t = 0; t < T0; ++t) {
+          v[t] = Pol::make(xv[t], ex);
+          if constexpr (Pol::SCALED) gsum = __fmaf_rn(v[t].hi, v[t].hi, gsum);
+        }
         contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
         const int base = tile_base<NN, D, 0>(lt);
 #pragma unroll
@@ -750,11 +824,19 @@ tile_kernel(const Problem p) {
         const int base = tile_base<NN, D, 0>(u);
         V v[T0];
 #pragma unroll
-        for (int t = 0; t < T0; ++t) v[t] = Pol::make(xs[base + tile_off<NN, D, 0>(t)], ex);
+        for (int t = 0; t < T0; ++t) {
+          v[t] = Pol::make(xs[base + tile_off<NN, D, 0>(t)], ex);
+          if constexpr (Pol::SCALED) gsum = __fmaf_rn(v[t].hi, v[t].hi, gsum);
+        }
         contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
 #pragma unroll
         for (int t = 0; t < T0; ++t) buf[slot<NN>(base + tile_off<NN, D, 0>(t))] = v[t];
       }
+    }
+    if constexpr (Pol::SCALED) {
+      gsum = warp_sum(gsum);
+      if ((lt & 31) == 0) atomicAdd(&nrm_k[MAXD], gsum);
+      gsum = 0.f;
     }
     fetch_next_factor();
     group_sync(g, G);  // S3: buf complete; the staging block is free
@@ -770,6 +852,7 @@ tile_kernel(const Problem p) {
 #pragma unroll
       for (int t = 0; t < TL; ++t) {
         const int q = base + tile_off<NN, D, LP>(t);
+        if constexpr (Pol::SCALED) gsum = __fmaf_rn(v[t].hi, v[t].hi, gsum);
         const Out y = Pol::finish(v[t], escale);
         if constexpr (SEG) {
           const Out a = first ? y : acc[q] + y;
@@ -783,8 +866,19 @@ tile_kernel(const Problem p) {
         }
       }
     }
+    if constexpr (Pol::SCALED) {
+      gsum = warp_sum(gsum);
+      if ((lt & 31) == 0) atomicAdd(&nrm_k[MAXD + 1], gsum);
+    }
     reduce_next_scale();
     group_sync(g, G);  // trailing: sA, buf reusable; next entry's scales final
+    if constexpr (Pol::SCALED) {
+      // cancellation guard (uniform over the group): redo in FP64 if rho_F < 1/4
+      if (!p.guard_off && guard_fails(nrm_k[MAXD + 1], nrm_k[MAXD], nrm_k, D, N)) {
+        guard_redo<Pol, NN, D, SEG>(p, ent, sA, buf, acc, yp, escale, last, lt, g);
+        group_sync(g, G);
+      }
+    }
   }
 }
 

@@ -195,6 +195,40 @@ def explicit_kron(d, m, nn, factors, lds, x):
     return out
 
 
+def kron_batched_extended(d, n, A, X, absolute=False):
+    """Y = kron(A_1, ..., A_d) X for every entry of a batched layout, evaluated
+    mode by mode (the recursion of kronmultv.hpp:19-148) in numpy's extended
+    precision (np.longdouble: 64-bit significand on x86, binary128 on aarch64),
+    returned in that precision.  A is (batch, d, n, n) with A[b, l, j, i] =
+    A_l(i, j) (column-major factors), X is (batch, n**d).  With absolute=True
+    it returns |K| |X|, the magnitude the rounding errors scale with."""
+    A = np.asarray(A, dtype=np.float64)
+    X = np.asarray(X, dtype=np.float64)
+    B = X.shape[0]
+    V = X.astype(np.longdouble).reshape((B,) + (n,) * d)
+    if absolute:
+        V = np.abs(V)
+    for m in range(d):
+        Am = A[:, m].astype(np.longdouble)  # [b, j, i]
+        if absolute:
+            Am = np.abs(Am)
+        W = np.moveaxis(V, 1 + m, -1)         # [b, ..., j]
+        W = np.einsum("bji,b...j->b...i", Am, W)
+        V = np.moveaxis(W, -1, 1 + m)
+    return V.reshape(B, -1)
+
+
+def xbatched_idx_extended(d, n, Apool, Xpool, ny, y_idx, x_idx, a_idx):
+    """Index-triple xbatched (pool layout of xbatched_idx, lda = n) in extended
+    precision: Y[y_idx[e]] += kron(Apool[l, a_idx[e, l]]) Xpool[x_idx[e]],
+    summed in np.longdouble from a zero Y and returned in that precision."""
+    Ab = np.stack([Apool[np.arange(d), a_idx[e]] for e in range(len(y_idx))])
+    contrib = kron_batched_extended(d, n, Ab, Xpool[x_idx])
+    Y = np.zeros((ny, n ** d), dtype=np.longdouble)
+    np.add.at(Y, y_idx, contrib)
+    return Y
+
+
 def kronmultv(d, m, nn, factors, lds, x, y):
     """One entry of the recursion, y += kron(...) x (x preserved)."""
     lib = oracle_lib()

@@ -16,7 +16,7 @@ def pytest_configure(config):
 def oracle():
     from oracle import pyoracle as po
 
-    po.build(ref=os.path.isdir("/root/reference"))
+    po.build(ref=True)  # oracle/Makefile skips the reference build where its tree is absent
     return po
 
 

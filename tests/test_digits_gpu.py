@@ -64,22 +64,43 @@ def test_digits_xbatched_vs_oracle(kmx, oracle, d, n, dist):
 
 @pytest.mark.parametrize("d,n", [(6, 4), (3, 16)])
 def test_digits_cancellation_goes_to_double_float(kmx, oracle, d, n):
-    """Entries whose result is far below the entry's scale (here: factors
-    whose rows sum to zero applied to a nearly constant X) are handed to the
-    double-float pass; mixed with ordinary entries on shared Y blocks."""
+    """Entries whose result cancels -- factors whose ROWS sum to zero (with
+    column-major storage A[l, p, j, i] = A_l(i, j) that is the sum over axis
+    2) applied to X = 1 + 1e-2 Z, which kron(...) nearly annihilates -- are
+    handed to the double-float pass (counted on the device) and recomputed
+    there in FP64 by its cancellation guard; mixed with ordinary entries on
+    shared Y blocks.  Against the recursion in extended precision: within
+    1e-13 per Y block, as plain FP64 is on the same data."""
     rng = np.random.default_rng(41)
     pool, nx, ny, ne = 16, 12, 6, 120
     N = n ** d
     Apool = rng.standard_normal((d, pool, n, n)) / 2
-    # half of the factor pool: rows sum to zero -> kron(...) annihilates constants
-    Apool[:, : pool // 2] -= Apool[:, : pool // 2].mean(axis=3, keepdims=True)
-    Xpool = 1.0 + 1e-9 * rng.standard_normal((nx, N))
-    Y0 = np.zeros((ny, N))
+    # half of the factor pool: zero row sums -> kron(...) annihilates constants
+    Apool[:, : pool // 2] -= Apool[:, : pool // 2].mean(axis=2, keepdims=True)
+    Xpool = 1.0 + 1e-2 * rng.standard_normal((nx, N))
     y_idx = rng.integers(0, ny, ne)
     x_idx = rng.integers(0, nx, ne)
     a_idx = rng.integers(0, pool, (ne, d))
-    y, yref = _pool_run(kmx, oracle, d, n, Apool, Xpool, Y0, y_idx, x_idx, a_idx)
-    assert blockwise_rel_err(y, yref) <= F64_TOL
+    cancels = np.any(a_idx < pool // 2, axis=1)  # one zero-row-sum factor suffices
+    Yx = oracle.xbatched_idx_extended(d, n, Apool, Xpool, ny, y_idx, x_idx, a_idx)
+    Yx = Yx.astype(np.float64)
+    Ad, Xd = torch.from_numpy(Apool).cuda(), torch.from_numpy(Xpool).cuda()
+    pA = kmx.pointer_array(Ad, ((np.arange(d)[None, :] * pool + a_idx) * n * n).ravel())
+    pX = kmx.pointer_array(Xd, x_idx * N)
+    out = {}
+    for form in ("plain", "digits"):
+        Yd = torch.zeros((ny, N), dtype=torch.float64, device="cuda")
+        kmx.read_redo_counters()
+        kmx.kronmult_xbatched(d, n, pA, n, pX, kmx.pointer_array(Yd, y_idx * N), None, ne,
+                              form=form)
+        torch.cuda.synchronize()
+        assert kmx.check_device_status() == 0
+        out[form] = (Yd.cpu().numpy(), kmx.read_redo_counters())
+    assert blockwise_rel_err(out["plain"][0], Yx) <= F64_TOL
+    y, (guard, handback) = out["digits"]
+    assert handback >= int(cancels.sum())
+    assert guard >= int(cancels.sum())
+    assert blockwise_rel_err(y, Yx) <= F64_TOL
 
 
 def test_digits_zero_blocks_contribute_nothing(kmx, oracle):

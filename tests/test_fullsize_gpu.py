@@ -213,7 +213,7 @@ def test_fullsize_precision_forms(kmx, d, n):
     A32, X32 = c["A"].float(), c["X"].float()
     Y32 = torch.zeros(c["X"].shape, dtype=torch.float32, device="cuda")
     pA, pX, pY = _pc_ptrs(c, A32, X32, Y32)
-    for form in (None, "tf32x3"):
+    for form in (None, "plain", "tf32x3"):
         Y32.zero_()
         kmx.kronmult_xbatched(d, n, pA, n, pX, pY, None, c["entries"], dtype=torch.float32,
                               form=form)
