@@ -54,13 +54,15 @@ def algorithmic_bytes(entries, nblocks, d=D, n=NN):
     return entries * (N * 8 + d * n * n * 8 + (d + 2) * 8) + nblocks * 2 * N * 8
 
 
-def make_workload(seed=SEED, entries=ENTRIES, nblocks=NBLOCKS, pool=POOL, d=D, n=NN):
+def make_workload(seed=SEED, entries=ENTRIES, nblocks=NBLOCKS, pool=POOL, d=D, n=NN, ny=None):
+    """nblocks X blocks and ny (default nblocks) Y blocks."""
+    ny = nblocks if ny is None else ny
     rng = np.random.default_rng(seed)
-    counts = rng.geometric(1.0 / MEAN_COUNT, nblocks).astype(np.int64)
+    counts = rng.geometric(1.0 / MEAN_COUNT, ny).astype(np.int64)
     # adjust to exactly `entries`, keeping every count >= 1
     diff = entries - int(counts.sum())
     while diff != 0:
-        idx = rng.integers(0, nblocks, abs(diff))
+        idx = rng.integers(0, ny, abs(diff))
         if diff > 0:
             np.add.at(counts, idx, 1)
         else:
@@ -68,7 +70,7 @@ def make_workload(seed=SEED, entries=ENTRIES, nblocks=NBLOCKS, pool=POOL, d=D, n
                 if counts[i] > 1:
                     counts[i] -= 1
         diff = entries - int(counts.sum())
-    y_idx = np.repeat(np.arange(nblocks, dtype=np.int32), counts)
+    y_idx = np.repeat(np.arange(ny, dtype=np.int32), counts)
     rng.shuffle(y_idx)
     x_idx = rng.integers(0, nblocks, entries, dtype=np.int32)
     a_idx = rng.integers(0, pool, (entries, d), dtype=np.int32)
@@ -247,12 +249,31 @@ def run_ours(args):
         dist.init_process_group("nccl")
 
     entries = args.entries
-    w = make_workload(seed=SEED + rank, entries=entries)
+    if world > 1:
+        # One batch of world x entries over world x 8192 Y blocks (X pool and
+        # factor pool replicated), partitioned by Y-block ownership: each rank
+        # runs the entries whose Y blocks it owns, against its own range of Y
+        # blocks, with no collective on the data path (weak scaling: about
+        # `entries` entries and 8192 Y blocks per rank).
+        from kronmult_gb300.shard import plan_by_y_owner
+
+        w = make_workload(seed=SEED, entries=entries * world, ny=NBLOCKS * world)
+        shards, ranges = plan_by_y_owner(w["y_idx"], world)
+        ids = np.sort(shards[rank])
+        y_lo, y_hi = ranges[rank]
+        w["y_idx"] = (w["y_idx"][ids] - y_lo).astype(np.int32)
+        w["x_idx"] = w["x_idx"][ids]
+        w["a_idx"] = w["a_idx"][ids]
+        entries = len(ids)
+        ny = y_hi - y_lo
+    else:
+        w = make_workload(seed=SEED, entries=entries)
+        ny = NBLOCKS
     N = NN ** D
     dev = torch.device("cuda", local)
     Ad = torch.from_numpy(w["Apool"]).to(dev)
     Xd = torch.from_numpy(w["Xpool"]).to(dev)
-    Yd = torch.zeros_like(Xd)
+    Yd = torch.zeros((ny, N), dtype=torch.float64, device=dev)
     y_idx = torch.from_numpy(w["y_idx"]).to(dev).long()
     x_idx = torch.from_numpy(w["x_idx"]).to(dev).long()
     a_idx = torch.from_numpy(w["a_idx"]).to(dev).long()
@@ -306,8 +327,8 @@ def run_ours(args):
     kmx.check_device_status()
 
     # accuracy: chosen vs plain on a fresh Y, and both vs the oracle on a sample
-    Yc = torch.zeros_like(Xd)
-    Yp = torch.zeros_like(Xd)
+    Yc = torch.zeros_like(Yd)
+    Yp = torch.zeros_like(Yd)
     _, _, pYc = ptrs(Ad, Xd, Yc)
     _, _, pYp = ptrs(Ad, Xd, Yp)
     step("auto", pYc)
@@ -316,8 +337,8 @@ def run_ours(args):
     num = torch.linalg.vector_norm(Yc - Yp, dim=1)
     den = torch.linalg.vector_norm(Yp, dim=1).clamp_min(1e-300)
     err_vs_plain = float((num / den).max().item())
-    Yd1 = torch.zeros_like(Xd)
-    Yd2 = torch.zeros_like(Xd)
+    Yd1 = torch.zeros_like(Yd)
+    Yd2 = torch.zeros_like(Yd)
     step("auto", ptrs(Ad, Xd, Yd1)[2], acc="deterministic")
     step("auto", ptrs(Ad, Xd, Yd2)[2], acc="deterministic")
     torch.cuda.synchronize()
@@ -331,7 +352,7 @@ def run_ours(args):
     err_dig_vs_plain = float((num / den).max().item())
     del Yd1, Yd2
 
-    total_flops = entries * flops_per_entry() * world
+    total_flops = args.entries * flops_per_entry() * world  # every rank's shard together
     value = total_flops / (ms * 1e-3) / 1e9
     value_plain = total_flops / (ms_plain * 1e-3) / 1e9
 
@@ -344,14 +365,14 @@ def run_ours(args):
     if not args.no_e2e:
         Ah = torch.from_numpy(w["Apool"]).pin_memory()
         Xh = torch.from_numpy(w["Xpool"]).pin_memory()
-        Yh = torch.zeros_like(Xh).pin_memory()
+        Yh = torch.zeros((ny, N), dtype=torch.float64).pin_memory()
         idx_h = torch.from_numpy(np.concatenate(
             [w["y_idx"], w["x_idx"], w["a_idx"].ravel()]).astype(np.int32)).pin_memory()
         # three buffer sets: step k+1's uploads need not wait for step k-1's
         # download, so slower host links do not stall the kernels
         NB = 3
-        Yout = [torch.empty_like(Xh).pin_memory() for _ in range(NB)]
-        bufs = [dict(A=torch.empty_like(Ad), X=torch.empty_like(Xd), Y=torch.empty_like(Xd),
+        Yout = [torch.empty_like(Yh).pin_memory() for _ in range(NB)]
+        bufs = [dict(A=torch.empty_like(Ad), X=torch.empty_like(Xd), Y=torch.empty_like(Yd),
                      idx=torch.empty(idx_h.numel(), dtype=torch.int32, device=dev))
                 for _ in range(NB)]
         h2d = (Ah.numel() + Xh.numel() + Yh.numel()) * 8 + idx_h.numel() * 4
@@ -364,8 +385,9 @@ def run_ours(args):
         s_out = [torch.cuda.Stream() for _ in range(NCH)]
         ev_out = [[torch.cuda.Event() for _ in range(NCH)] for _ in range(NB)]
         started = [False] * NB
-        rows = Xh.shape[0]
+        rows, yrows = Xh.shape[0], Yh.shape[0]
         cuts = [rows * c // NCH for c in range(NCH + 1)]
+        ycuts = [yrows * c // NCH for c in range(NCH + 1)]
 
         cmp_events = []  # (start, end) of each timed step's device work on the compute stream
 
@@ -379,9 +401,10 @@ def run_ours(args):
                     for ev in ev_out[b]:
                         st.wait_event(ev)
                 lo, hi = cuts[c], cuts[c + 1]
+                ylo, yhi = ycuts[c], ycuts[c + 1]
                 with torch.cuda.stream(st):
                     B["X"][lo:hi].copy_(Xh[lo:hi], non_blocking=True)
-                    B["Y"][lo:hi].copy_(Yh[lo:hi], non_blocking=True)
+                    B["Y"][ylo:yhi].copy_(Yh[ylo:yhi], non_blocking=True)
                     if c == 0:
                         B["A"].copy_(Ah, non_blocking=True)
                         B["idx"].copy_(idx_h, non_blocking=True)
@@ -395,9 +418,9 @@ def run_ours(args):
                     c0 = torch.cuda.Event(enable_timing=True)
                     c0.record(s_cmp)
                 idx = B["idx"]
-                nb = B["X"].shape[0]
+                nb, nyb = B["X"].shape[0], B["Y"].shape[0]
                 qA, qX, qY = kmx.xbatched_build(
-                    D, B["A"], POOL * NN * NN, NN * NN, POOL, B["X"], N, nb, B["Y"], N, nb,
+                    D, B["A"], POOL * NN * NN, NN * NN, POOL, B["X"], N, nb, B["Y"], N, nyb,
                     idx[:entries], idx[entries:2 * entries], idx[2 * entries:], stream=s_cmp)
                 kmx.kronmult_xbatched(D, NN, qA, NN, qX, qY, None, entries, stream=s_cmp)
                 ev_cmp = torch.cuda.Event(enable_timing=timed)
@@ -405,7 +428,7 @@ def run_ours(args):
                 if timed:
                     cmp_events.append((c0, ev_cmp))
             for c in range(NCH):
-                lo, hi = cuts[c], cuts[c + 1]
+                lo, hi = ycuts[c], ycuts[c + 1]
                 s_out[c].wait_event(ev_cmp)
                 with torch.cuda.stream(s_out[c]):
                     Yout[b][lo:hi].copy_(B["Y"][lo:hi], non_blocking=True)
@@ -459,7 +482,7 @@ def run_ours(args):
     L.kmx_probe_fma_rate(0, C.byref(r32))
     fp64_tflops = 2 * r64.value / 1e12
     fp32_tflops = 2 * r32.value / 1e12
-    alg_bytes = algorithmic_bytes(entries, NBLOCKS)
+    alg_bytes = algorithmic_bytes(entries, ny)  # this rank's launch
     achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
     tpe = profile_traffic()
     roofline = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": peaks["hbm_gbs"],
@@ -499,11 +522,14 @@ def run_ours(args):
         "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "d": D, "n": NN, "entries": entries,
-                   "x_blocks": NBLOCKS, "y_blocks": NBLOCKS, "factor_pool": POOL,
+        "config": {"workload": WORKLOAD, "d": D, "n": NN, "entries": args.entries * world,
+                   "x_blocks": NBLOCKS, "y_blocks": NBLOCKS * world, "factor_pool": POOL,
                    "accumulate": "atomic", "form_chosen": "split (double-float)",
                    "l2": "inputs larger than L2 (256 MiB X and Y pools), no flush",
-                   "seed": SEED, "parallelism": f"entries sharded per GPU x{world}"},
+                   "seed": SEED,
+                   "parallelism": ("one GPU" if world == 1 else
+                                   f"Y-block ownership shards of one batch x{world} "
+                                   "(no data-path collective)")},
         "plain": {"value": round(value_plain, 3), "unit": "GFLOP/s", "ms_per_step": round(ms_plain, 4)},
         "deterministic": {"value": round(total_flops / (ms_det * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
                           "ms_per_step": round(ms_det, 4), "bitwise_repeatable": det_bitwise,

@@ -96,7 +96,9 @@ typedef enum kmx_accumulate {
 typedef enum kmx_engine {
   KMX_ENGINE_TUNED = 0,    /* the committed tuning table's choice for (form, d, n) */
   KMX_ENGINE_PER_MODE = 1, /* one mode contraction per pass over shared memory */
-  KMX_ENGINE_TILED = 2     /* register tiles of one or two modes, TMA-prefetched X */
+  KMX_ENGINE_TILED = 2,    /* register tiles of one or two modes, TMA-prefetched X */
+  KMX_ENGINE_SMALL = 3     /* d <= 3 with n^d <= 256: many entries per CTA, staged with
+                              128-bit loads, one thread per output element and mode */
 } kmx_engine;
 
 typedef struct kmx_options {

@@ -5,9 +5,11 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "kmx_engine.cuh"
+#include "kmx_small.cuh"
 #include "kmx_tile.cuh"
 
 namespace kmx {
@@ -22,7 +24,7 @@ struct LaunchHint {
   int group_threads;
   int groups_per_cta;
   int max_ctas;  // cap on the grid (0 = fill the GPU)
-  int engine;    // 0 choose, 1 per-mode kernels only, 2 register-tiled kernels only
+  int engine;    // 0 choose, 1 per-mode kernels, 2 register-tiled kernels, 3 small-entry kernels
 };
 
 struct DeviceInfo {
@@ -86,17 +88,25 @@ const void* pick_sq(int nn) {
 // Register-tiled kernels (kmx_tile.cuh) for square NN in 2..8, d in 3..6,
 // where one entry's intermediate fits in shared memory.
 // ---------------------------------------------------------------------------
-template <typename T, int FORM>
+template <typename T, int FORM, int NN, int D>
 struct TilePol {
   using type = tile::PlainPolicy<T>;
 };
-template <typename T>
-struct TilePol<T, FORM_SPLIT> {
-  using type = tile::SplitPolicy;
+// Double-float on packed FP32 pairs where it measured faster on GB300 (same
+// box, same build, batched layout): even n <= 8 with one tile per thread in
+// the first phase, e.g. d=6 n=4 +10 %, d=3 n=8 +19 %, d=4 n=6 +11 %.  Odd n
+// pads a zero row to every row pair (a third more arithmetic for n = 3:
+// d=5 n=3 -16 %), and with several tiles per thread the packed operands
+// spill (d=5 n=7 -16 %, d=5 n=5 -11 %): those keep the scalar form, as does
+// n = 16, whose broadcast operands would not fit in registers.
+template <typename T, int NN, int D>
+struct TilePol<T, FORM_SPLIT, NN, D> {
+  using type = typename std::conditional<tile::packed_pays(NN, D), tile::PackedSplitPolicy,
+                                         tile::SplitPolicy>::type;
 };
 // FP32 / BF16 storage, FP32 arithmetic, FP64 Y (T is the storage type)
-template <typename T>
-struct TilePol<T, FORM_WIDE> {
+template <typename T, int NN, int D>
+struct TilePol<T, FORM_WIDE, NN, D> {
   using type = tile::WidePolicy<T>;
 };
 
@@ -108,7 +118,7 @@ struct TileKernel {
 
 template <typename T, int FORM, int NN, int D, bool SEG>
 TileKernel tile_entry() {
-  using Pol = typename TilePol<T, FORM>::type;
+  using Pol = typename TilePol<T, FORM, NN, D>::type;
   TileKernel k;
   constexpr int bytes = tile::group_smem_bytes<Pol, NN, D, SEG>();
   if constexpr (bytes <= 227 * 1024) {
@@ -174,6 +184,87 @@ inline cudaError_t launch_tile(Problem& p, const TileKernel& k, const LaunchHint
   p.group_smem = k.group_smem;
   void* args[] = {&p};
   return cudaLaunchKernel(k.func, dim3(grid), dim3(E * G), args, smem, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Small-entry kernels (kmx_small.cuh): d <= 3, n^d <= 256, many entries per CTA.
+// ---------------------------------------------------------------------------
+template <typename T, int FORM>
+struct SmallPol {
+  using type = small::SmallPlain<T, false>;
+};
+template <typename T>
+struct SmallPol<T, FORM_SPLIT> {
+  using type = small::SmallSplit;
+};
+template <typename T>
+struct SmallPol<T, FORM_REF32> {
+  using type = small::SmallPlain<T, true>;
+};
+
+struct SmallKernel {
+  const void* func = nullptr;
+  int smem = 0;
+};
+
+template <typename T, int FORM, int NN, int D>
+SmallKernel small_entry() {
+  SmallKernel k;
+  if constexpr (small::supported(NN, D)) {
+    using Pol = typename SmallPol<T, FORM>::type;
+    k.func = reinterpret_cast<const void*>(&small::small_kernel<Pol, NN, D>);
+    k.smem = small::Layout<Pol, NN, D>::BYTES;
+  }
+  return k;
+}
+
+template <typename T, int FORM, int NN>
+SmallKernel small_for_d(int d) {
+  switch (d) {
+    case 1: return small_entry<T, FORM, NN, 1>();
+    case 2: return small_entry<T, FORM, NN, 2>();
+    case 3: return small_entry<T, FORM, NN, 3>();
+    default: return SmallKernel();
+  }
+}
+
+template <typename T, int FORM>
+SmallKernel pick_small(int nn, int d) {
+  if constexpr (FORM == FORM_WIDE) {
+    return SmallKernel();
+  } else {
+    switch (nn) {
+      case 2: return small_for_d<T, FORM, 2>(d);
+      case 3: return small_for_d<T, FORM, 3>(d);
+      case 4: return small_for_d<T, FORM, 4>(d);
+      case 5: return small_for_d<T, FORM, 5>(d);
+      case 6: return small_for_d<T, FORM, 6>(d);
+      case 7: return small_for_d<T, FORM, 7>(d);
+      case 8: return small_for_d<T, FORM, 8>(d);
+      case 16: return small_for_d<T, FORM, 16>(d);
+      default: return SmallKernel();
+    }
+  }
+}
+
+inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHint& hint,
+                                cudaStream_t stream) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo di = device_info(dev);
+  err = ensure_smem(k.func, dev, k.smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.func, small::THREADS, k.smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  long long cap = (long long)di.sms * per_sm;
+  if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
+  // chunks of the launch: an upper bound when the count is on the device
+  const int grid = (int)(cap < (long long)p.count ? cap : (p.count > 0 ? p.count : 1));
+  void* args[] = {&p};
+  return cudaLaunchKernel(k.func, dim3(grid), dim3(small::THREADS), args, k.smem, stream);
 }
 
 // Bytes of shared memory one group needs (on-chip intermediate included).
@@ -260,6 +351,10 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   const bool square = is_square(p);
   const int nn = p.n[0];
   const bool seg = p.seg_entries != nullptr;
+  if (!seg && square && hint.engine == 3) {
+    const SmallKernel sk = pick_small<T, FORM>(nn, p.d);
+    if (sk.func) return launch_small(p, sk, hint, stream);
+  }
   if constexpr (FORM != FORM_REF32) {
     if (seg) {
       // deterministic mode: the register-tiled segment kernels where they

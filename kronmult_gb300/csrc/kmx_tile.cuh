@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "kmx_engine.cuh"
+#include "kmx_pack.cuh"
 
 namespace kmx {
 namespace tile {
@@ -65,6 +66,11 @@ __host__ __device__ constexpr int group_threads(int NN, int D) {
              : (round32(ipow(NN, D) / tile_size(NN, D, 0)) < 32
                     ? 32
                     : round32(ipow(NN, D) / tile_size(NN, D, 0)));
+}
+// whether the packed double-float policy is used for (NN, D): even NN <= 8
+// with one first-phase tile per thread (see TilePol in kmx_launch.cuh)
+__host__ __device__ constexpr bool packed_pays(int NN, int D) {
+  return NN % 2 == 0 && NN <= 8 && ipow(NN, D) / tile_size(NN, D, 0) <= 512;
 }
 __host__ __device__ constexpr int factors_per_thread(int NN, int D) {
   return (D * NN * NN + group_threads(NN, D) - 1) / group_threads(NN, D);
@@ -113,8 +119,28 @@ __device__ __forceinline__ constexpr int tile_off(int e) {
 // Arithmetic policies.
 // ---------------------------------------------------------------------------
 
+// Factor storage of the policies with one value per factor element: factor
+// l is NN*NN values of V, row-major (row = output index).
+template <typename V>
+struct FlatFactors {
+  static constexpr bool PACKED = false;
+  template <int NN>
+  __host__ __device__ static constexpr int factor_bytes() {
+    return NN * NN * (int)sizeof(V);
+  }
+  template <int NN>
+  __device__ __forceinline__ static const void* factor(const unsigned char* base, int l) {
+    return base + (size_t)l * factor_bytes<NN>();
+  }
+  // element idx = l*NN*NN + r*NN + j
+  template <int NN>
+  __device__ __forceinline__ static void store_factor(unsigned char* base, int idx, V a) {
+    reinterpret_cast<V*>(base)[idx] = a;
+  }
+};
+
 // Double-float with per-entry power-of-two scaling (see kmx_engine.cuh).
-struct SplitPolicy {
+struct SplitPolicy : FlatFactors<df> {
   using In = double;
   using V = df;
   using Out = double;
@@ -167,8 +193,33 @@ struct SplitPolicy {
   }
 };
 
+// Double-float on packed FP32 pairs (kmx_pack.cuh): two output rows per
+// instruction.  Factors are stored as row pairs (high, low and negated high
+// parts); the arithmetic per value is that of SplitPolicy.
+struct PackedSplitPolicy : SplitPolicy {
+  static constexpr bool PACKED = true;
+  template <int NN>
+  __host__ __device__ static constexpr int factor_bytes() {
+    return pk2::factor_u64<NN>() * 8;
+  }
+  template <int NN>
+  __device__ __forceinline__ static const void* factor(const unsigned char* base, int l) {
+    return base + (size_t)l * factor_bytes<NN>();
+  }
+  template <int NN>
+  __device__ __forceinline__ static void store_factor(unsigned char* base, int idx, df a) {
+    constexpr int NN2 = NN * NN;
+    const int l = idx / NN2, r = (idx - l * NN2) / NN, j = idx - l * NN2 - r * NN;
+    float* f = reinterpret_cast<float*>(base + (size_t)l * factor_bytes<NN>()) +
+               ((r >> 1) * NN + j) * 6 + (r & 1);
+    f[0] = a.hi;
+    f[2] = a.lo;
+    f[4] = -a.hi;
+  }
+};
+
 template <typename T>
-struct PlainPolicy {
+struct PlainPolicy : FlatFactors<T> {
   using In = T;
   using V = T;
   using Out = T;
@@ -189,7 +240,7 @@ struct PlainPolicy {
 // run in FP32, and each contribution is widened exactly to FP64 before it is
 // added to the (FP64) Y block, so overlapping contributions accumulate in FP64.
 template <typename TIn>
-struct WidePolicy {
+struct WidePolicy : FlatFactors<float> {
   using In = TIn;
   using V = float;
   using Out = double;
@@ -210,12 +261,102 @@ struct WidePolicy {
   __device__ __forceinline__ static double finish(V o, int) { return SplitPolicy::to_f64(o, 0); }
 };
 
-// Contract the tile's mode(s) in registers.  sA points at the phase's
-// factor(s) in shared memory, rows of NN values of V.
+// Packed double-float contraction of a tile (PackedSplitPolicy): the dot
+// products of output rows (2rp, 2rp+1) share one instruction stream.
+template <int NN, bool PAIR>
+__device__ __forceinline__ void contract_tile_packed(df* v, const pk2::RowPair* Fa,
+                                                     const pk2::RowPair* Fb) {
+  using pk2::u64;
+  constexpr int RP = pk2::row_pairs<NN>();
+  pk2::PackedRows<NN> A;
+  A.load(Fa);
+  if constexpr (PAIR) {
+    // first mode: columns (fixed second index), rows paired
+#pragma unroll
+    for (int c = 0; c < NN; ++c) {
+      u64 vh[NN], vl[NN], oh[RP], ol[RP];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        vh[j] = pk2::bcast(v[j * NN + c].hi);
+        vl[j] = pk2::bcast(v[j * NN + c].lo);
+      }
+#pragma unroll
+      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+#pragma unroll
+      for (int rp = 0; rp < RP; ++rp) {
+        float h0, h1, l0, l1;
+        pk2::unpack(oh[rp], h0, h1);
+        pk2::unpack(ol[rp], l0, l1);
+        v[2 * rp * NN + c].hi = h0;
+        v[2 * rp * NN + c].lo = l0;
+        if (2 * rp + 1 < NN) {
+          v[(2 * rp + 1) * NN + c].hi = h1;
+          v[(2 * rp + 1) * NN + c].lo = l1;
+        }
+      }
+    }
+    A.load(Fb);
+    // second mode: rows (fixed first index), output columns paired
+#pragma unroll
+    for (int r0 = 0; r0 < NN; ++r0) {
+      u64 vh[NN], vl[NN], oh[RP], ol[RP];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        vh[j] = pk2::bcast(v[r0 * NN + j].hi);
+        vl[j] = pk2::bcast(v[r0 * NN + j].lo);
+      }
+#pragma unroll
+      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+#pragma unroll
+      for (int rp = 0; rp < RP; ++rp) {
+        float h0, h1, l0, l1;
+        pk2::unpack(oh[rp], h0, h1);
+        pk2::unpack(ol[rp], l0, l1);
+        v[r0 * NN + 2 * rp].hi = h0;
+        v[r0 * NN + 2 * rp].lo = l0;
+        if (2 * rp + 1 < NN) {
+          v[r0 * NN + 2 * rp + 1].hi = h1;
+          v[r0 * NN + 2 * rp + 1].lo = l1;
+        }
+      }
+    }
+  } else {
+    u64 vh[NN], vl[NN], oh[RP], ol[RP];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) {
+      vh[j] = pk2::bcast(v[j].hi);
+      vl[j] = pk2::bcast(v[j].lo);
+    }
+#pragma unroll
+    for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+#pragma unroll
+    for (int rp = 0; rp < RP; ++rp) {
+      float h0, h1, l0, l1;
+      pk2::unpack(oh[rp], h0, h1);
+      pk2::unpack(ol[rp], l0, l1);
+      v[2 * rp].hi = h0;
+      v[2 * rp].lo = l0;
+      if (2 * rp + 1 < NN) {
+        v[2 * rp + 1].hi = h1;
+        v[2 * rp + 1].lo = l1;
+      }
+    }
+  }
+}
+
+// Contract the tile's mode(s) in registers.  Afirst / Asecond point at the
+// phase's factor(s) in shared memory (layout of the policy's factor storage).
 template <class Pol, int NN, bool PAIR>
-__device__ __forceinline__ void contract_tile(typename Pol::V* v, const typename Pol::V* Afirst,
-                                              const typename Pol::V* Asecond) {
+__device__ __forceinline__ void contract_tile(typename Pol::V* v, const void* Afirst_,
+                                              const void* Asecond_) {
   using V = typename Pol::V;
+  if constexpr (Pol::PACKED) {
+    contract_tile_packed<NN, PAIR>(v, static_cast<const pk2::RowPair*>(Afirst_),
+                                   static_cast<const pk2::RowPair*>(Asecond_));
+    return;
+  } else {
+  const V* Afirst = static_cast<const V*>(Afirst_);
+  const V* Asecond = static_cast<const V*>(Asecond_);
   Rows<V, NN> A;
   A.load(Afirst);
   if constexpr (PAIR) {
@@ -248,11 +389,12 @@ __device__ __forceinline__ void contract_tile(typename Pol::V* v, const typename
 #pragma unroll
     for (int r = 0; r < NN; ++r) v[r] = out[r];
   }
+  }
 }
 
 // One middle phase P over all tiles of the group: shared memory -> shared memory.
 template <class Pol, int NN, int D, int G, int P>
-__device__ __forceinline__ void middle_phase(typename Pol::V* buf, const typename Pol::V* sA,
+__device__ __forceinline__ void middle_phase(typename Pol::V* buf, const unsigned char* sA,
                                              int lt) {
   using V = typename Pol::V;
   constexpr int a = phase_a(NN, D, P);
@@ -264,14 +406,15 @@ __device__ __forceinline__ void middle_phase(typename Pol::V* buf, const typenam
     V v[T];
 #pragma unroll
     for (int e = 0; e < T; ++e) v[e] = buf[slot<NN>(base + tile_off<NN, D, P>(e))];
-    contract_tile<Pol, NN, (b >= 0)>(v, sA + a * NN * NN, sA + (b >= 0 ? b : a) * NN * NN);
+    contract_tile<Pol, NN, (b >= 0)>(v, Pol::template factor<NN>(sA, a),
+                                     Pol::template factor<NN>(sA, b >= 0 ? b : a));
 #pragma unroll
     for (int e = 0; e < T; ++e) buf[slot<NN>(base + tile_off<NN, D, P>(e))] = v[e];
   }
 }
 
 template <class Pol, int NN, int D, int G, int P>
-__device__ __forceinline__ void middle_phases(typename Pol::V* buf, const typename Pol::V* sA,
+__device__ __forceinline__ void middle_phases(typename Pol::V* buf, const unsigned char* sA,
                                               int lt, int g) {
   if constexpr (P < num_phases(NN, D) - 1) {
     middle_phase<Pol, NN, D, G, P>(buf, sA, lt);
@@ -369,9 +512,13 @@ __device__ __forceinline__ const T* a_ptr(const Problem& p, long long ent, int l
 //   [intermediate: buffer_slots x V]
 //   [segment accumulator: N x Out]   (deterministic mode only)
 // ---------------------------------------------------------------------------
+// factor storage first; it also holds MAXD*NN*NN doubles for the FP64
+// evaluation of an entry (nonfinite_entry, guard_redo)
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_ints() {
-  return MAXD * NN * NN * (int)sizeof(typename Pol::V);
+  return (MAXD * Pol::template factor_bytes<NN>() > MAXD * NN * NN * 8
+              ? MAXD * Pol::template factor_bytes<NN>()
+              : MAXD * NN * NN * 8 + 15) / 16 * 16;
 }
 template <class Pol, int NN, int D>
 __host__ __device__ constexpr int off_desc() {
@@ -441,14 +588,13 @@ __device__ __noinline__ void nonfinite_entry(const Problem& p, long long ent, do
 // last phase leaves unchanged, by the same arithmetic, so bitwise the same
 // values -- and add the plain FP64 result instead.  Out of line: rarely taken.
 template <class Pol, int NN, int D, bool SEG>
-__device__ __noinline__ void guard_redo(const Problem& p, long long ent, typename Pol::V* sA,
+__device__ __noinline__ void guard_redo(const Problem& p, long long ent, unsigned char* sA,
                                         typename Pol::V* buf, typename Pol::Out* acc,
                                         typename Pol::Out* yp, int escale, bool last, int lt,
                                         int g) {
   using V = typename Pol::V;
   using Out = typename Pol::Out;
   constexpr int G = group_threads(NN, D);
-  constexpr int NN2 = NN * NN;
   constexpr int LP = num_phases(NN, D) - 1;
   constexpr int TL = tile_size(NN, D, LP);
   constexpr int NTL = ipow(NN, D) / TL;
@@ -460,7 +606,8 @@ __device__ __noinline__ void guard_redo(const Problem& p, long long ent, typenam
     V v[TL];
 #pragma unroll
     for (int t = 0; t < TL; ++t) v[t] = buf[slot<NN>(base + tile_off<NN, D, LP>(t))];
-    contract_tile<Pol, NN, PAIRL>(v, sA + aL * NN2, sA + bL * NN2);
+    contract_tile<Pol, NN, PAIRL>(v, Pol::template factor<NN>(sA, aL),
+                                  Pol::template factor<NN>(sA, bL));
 #pragma unroll
     for (int t = 0; t < TL; ++t) {
       const int q = base + tile_off<NN, D, LP>(t);
@@ -540,7 +687,7 @@ tile_kernel(const Problem p) {
   const int lt = threadIdx.x - g * G;
   if (g >= E) return;
   unsigned char* gb = smem + (size_t)g * group_smem_bytes<Pol, NN, D, SEG>();
-  V* sA = reinterpret_cast<V*>(gb);
+  unsigned char* sA = gb;  // factor storage (layout of the policy)
   int* sExp = reinterpret_cast<int*>(gb + off_ints<Pol, NN, D>());  // [2][MAXD+1]
   int* sFlag = sExp + 2 * (MAXD + 1);                                 // [2]
   int* sMode = sFlag + 2;                                             // [1]
@@ -581,6 +728,10 @@ tile_kernel(const Problem p) {
 
   if (lt < 2 * (MAXD + 1) + 4) sExp[lt] = 0;
   if (lt < 2 * NRM_STRIDE) sNrm[lt] = 0.f;
+  if constexpr (Pol::PACKED) {
+    // the pad row of an odd NN stays zero (entries write real rows only)
+    for (int i = lt; i < off_ints<Pol, NN, D>() / 4; i += G) reinterpret_cast<float*>(sA)[i] = 0.f;
+  }
   if (lt == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
@@ -660,7 +811,7 @@ tile_kernel(const Problem p) {
     for (int f = 0; f < FPT; ++f) {
       if (fthr[f]) {
         const V a = Pol::make(af[f], Pol::SCALED ? ex_k[al[f]] : 0);
-        sA[lt + f * G] = a;
+        Pol::template store_factor<NN>(sA, lt + f * G, a);
         if constexpr (Pol::SCALED) atomicAdd(&nrm_k[al[f]], a.hi * a.hi);
       }
     }
@@ -814,7 +965,8 @@ tile_kernel(const Problem p) {
           v[t] = Pol::make(xv[t], ex);
           if constexpr (Pol::SCALED) gsum = __fmaf_rn(v[t].hi, v[t].hi, gsum);
         }
-        contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
+        contract_tile<Pol, NN, PAIR0>(v, Pol::template factor<NN>(sA, a0),
+                                      Pol::template factor<NN>(sA, b0));
         const int base = tile_base<NN, D, 0>(lt);
 #pragma unroll
         for (int t = 0; t < T0; ++t) buf[slot<NN>(base + tile_off<NN, D, 0>(t))] = v[t];
@@ -828,7 +980,8 @@ tile_kernel(const Problem p) {
           v[t] = Pol::make(xs[base + tile_off<NN, D, 0>(t)], ex);
           if constexpr (Pol::SCALED) gsum = __fmaf_rn(v[t].hi, v[t].hi, gsum);
         }
-        contract_tile<Pol, NN, PAIR0>(v, sA + a0 * NN2, sA + b0 * NN2);
+        contract_tile<Pol, NN, PAIR0>(v, Pol::template factor<NN>(sA, a0),
+                                      Pol::template factor<NN>(sA, b0));
 #pragma unroll
         for (int t = 0; t < T0; ++t) buf[slot<NN>(base + tile_off<NN, D, 0>(t))] = v[t];
       }
@@ -848,7 +1001,8 @@ tile_kernel(const Problem p) {
       V v[TL];
 #pragma unroll
       for (int t = 0; t < TL; ++t) v[t] = buf[slot<NN>(base + tile_off<NN, D, LP>(t))];
-      contract_tile<Pol, NN, PAIRL>(v, sA + aL * NN2, sA + bL * NN2);
+      contract_tile<Pol, NN, PAIRL>(v, Pol::template factor<NN>(sA, aL),
+                                    Pol::template factor<NN>(sA, bL));
 #pragma unroll
       for (int t = 0; t < TL; ++t) {
         const int q = base + tile_off<NN, D, LP>(t);

@@ -5,8 +5,9 @@ current GPU and write the committed tuning table ``tune_table.json``.
 
 For each form (FP64 plain, FP64 split, FP32) and square shape (d = 1..6,
 n = 2..8 and 16 where an entry has at most 2^18 elements) the batched entry
-point is timed with each engine (per-mode kernels, register-tiled kernels)
-on about 256 MiB of X; the fastest engine is recorded.  For FP64 the
+point is timed with each engine (per-mode kernels, register-tiled kernels,
+small-entry kernels) on about 256 MiB of X; the fastest engine is recorded.
+FP32 rows time FP32 fused multiply-add (form PLAIN), the kernels they tune.  For FP64 the
 automatic form is the faster of plain and split.  ``build.py`` compiles the
 table into ``csrc/kmx_tune_table.h``; the library consults it whenever the
 caller leaves ``engine`` / ``form`` on their automatic settings.
@@ -23,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "tune_table.json")
 
 FORM_CODES = {"plain": 1, "split": 2, "f32": 3}
-ENGINE_CODES = {"per_mode": 1, "tiled": 2}
+ENGINE_CODES = {"per_mode": 1, "tiled": 2, "small": 3}
 
 
 def shapes():
@@ -42,7 +43,7 @@ def time_one(kmx, torch, d, n, form, engine, target_bytes, reps):
     X = torch.randn((batch, N), dtype=dt, device="cuda")
     Y = torch.zeros_like(X)
     W = torch.zeros_like(X) if N * esz > 200 * 1024 else None
-    f = None if form == "f32" else form
+    f = "plain" if form == "f32" else form  # FP32 rows time the FMA kernels they tune
 
     def call():
         kmx.kronmult_batched(d, n, A, X, Y, W, batch, form=f, engine=engine)
@@ -65,6 +66,10 @@ def has_tile(d, n):
     return (3 <= d <= 6 and 2 <= n <= 8) or (d == 3 and n == 16)
 
 
+def has_small(d, n):
+    return d <= 3 and n ** d <= 256
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=TABLE)
@@ -84,8 +89,10 @@ def main(argv=None):
             if form == "split" and not (2 <= n <= 8 or n == 16):
                 continue
             res = {}
-            for engine in ("per_mode", "tiled"):
+            for engine in ("per_mode", "tiled", "small"):
                 if engine == "tiled" and not has_tile(d, n):
+                    continue
+                if engine == "small" and not has_small(d, n):
                     continue
                 try:
                     res[engine] = time_one(kmx, torch, d, n, form, engine, target, reps)
