@@ -616,8 +616,12 @@ def run_mixed(args):
     W = torch.empty(2 * 262144 * 512, dtype=torch.float64, device=dev)
     flops = float((2.0 * d * n.astype(np.float64) ** (d + 1)).sum())
     res = {}
-    for form in ("auto", "plain"):
-        call = lambda: kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form)
+    # auto: one tuned launch per class (the default); persistent: one launch
+    # over every class fed by a device work queue (generic double-float kernel)
+    for name, form, engine in (("auto", "auto", None), ("plain", "plain", None),
+                               ("persistent", "auto", "persistent")):
+        call = lambda: kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form,
+                                          engine=engine)
         ms_eager = _events_time(torch, call, max(2, args.steps // 3), 2)
         # 100-call sequence as one CUDA graph
         s = torch.cuda.Stream()
@@ -626,10 +630,11 @@ def run_mixed(args):
         with torch.cuda.stream(s):
             with torch.cuda.graph(graph, stream=s):
                 for _ in range(100):
-                    kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form, stream=s)
+                    kmx.kronmult_mixed(dims, pA, aoff_d, pX, pY, classes, W, form=form,
+                                       engine=engine, stream=s)
         torch.cuda.current_stream().wait_stream(s)
         ms_graph = _events_time(torch, graph.replay, 2, 1) / 100
-        res[form] = {"gflops_graph": round(flops / (ms_graph * 1e-3) / 1e9, 2),
+        res[name] = {"gflops_graph": round(flops / (ms_graph * 1e-3) / 1e9, 2),
                      "ms_per_call_graph": round(ms_graph, 4),
                      "gflops_eager": round(flops / (ms_eager * 1e-3) / 1e9, 2),
                      "ms_per_call_eager": round(ms_eager, 4)}
@@ -649,6 +654,7 @@ def run_mixed(args):
                       "workload": "mixed", "instances": count, "classes": len(classes),
                       "total_gflop_per_call": round(flops / 1e9, 2),
                       "chosen": res["auto"], "plain": res["plain"],
+                      "persistent_one_launch": res["persistent"],
                       "rel_err_chosen_vs_plain_512_instances": err, "data": "synthetic"}))
 
 

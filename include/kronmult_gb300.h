@@ -97,8 +97,21 @@ typedef enum kmx_engine {
   KMX_ENGINE_TUNED = 0,    /* the committed tuning table's choice for (form, d, n) */
   KMX_ENGINE_PER_MODE = 1, /* one mode contraction per pass over shared memory */
   KMX_ENGINE_TILED = 2,    /* register tiles of one or two modes, TMA-prefetched X */
-  KMX_ENGINE_SMALL = 3     /* d <= 3 with n^d <= 256: many entries per CTA, staged with
+  KMX_ENGINE_SMALL = 3,    /* d <= 3 with n^d <= 256: many entries per CTA, staged with
                               128-bit loads, one thread per output element and mode */
+  KMX_ENGINE_PERSISTENT = 4 /* kmx_kronmult_mixed_f64 with form AUTO or SPLIT and atomic
+                              accumulation: ONE persistent launch over every class, instances
+                              taken from a device work queue in class order, each run by the
+                              generic double-float kernel with its own (d, n) (the default runs
+                              one tuned launch per class, measured faster); other calls treat
+                              it as TUNED */,
+  KMX_ENGINE_CLUSTER = 5   /* double-float entries beyond one SM's shared memory (square
+                              d=5 n=8, d=6 n=6..8, atomic accumulation): a thread-block
+                              cluster of n CTAs per (entry, i1) sharing mode 2 through
+                              distributed shared memory, no workspace.  Every engine takes
+                              it for these shapes when the call passes no workspace; with
+                              a workspace the per-mode kernels run (measured faster) unless
+                              this engine is asked for; other shapes treat it as TUNED */
 } kmx_engine;
 
 typedef struct kmx_options {
@@ -423,7 +436,9 @@ int kmx_check_device_status(kmx_stream_t stream, int* flags);
  * rho_F = ||KX|| sqrt(prod n_l) / (prod_l ||A_l||_F ||X||) falls below 1/4,
  * where double-float's ~2^-48 relative to |K||X| would lose more accuracy than
  * FP64); counts[1]: entries the digits form handed to the double-float pass.
- * Synchronises the stream; counts may be NULL (then only cleared). */
+ * The cluster kernels (double-float entries beyond one SM's shared memory)
+ * decide per block of n^(d-2) outputs and count blocks.  Synchronises the
+ * stream; counts may be NULL (then only cleared). */
 int kmx_read_redo_counters(kmx_stream_t stream, unsigned long long* counts);
 
 /* The last CUDA error code seen by the library on this thread. */

@@ -259,6 +259,8 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     return e ? std::atoi(e) : 0;
   }();
   h.engine = o.engine ? o.engine : engine_env;
+  if (h.engine == KMX_ENGINE_PERSISTENT) h.engine = 0;  // mixed-shape calls only
+  if (h.engine == KMX_ENGINE_CLUSTER && !is_f64) h.engine = 0;
   cudaError_t e;
   const bool sq = is_square(p);
   if (wide_in) {
@@ -287,6 +289,12 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
   } else {
     if (o.form == KMX_FORM_SPLIT_RAW) p.guard_off = 1;
     int form = resolve_f64_form(p, o.form);
+    // the cluster engine exists for double-float entries beyond one SM's
+    // shared memory (square d=5 n=8, d=6 n=6..8); elsewhere it is TUNED
+    if (h.engine == KMX_ENGINE_CLUSTER &&
+        !(sq && form == KMX_FORM_SPLIT &&
+          ((p.d == 5 && p.n[0] == 8) || (p.d == 6 && p.n[0] >= 6 && p.n[0] <= 8))))
+      h.engine = 0;
     h.engine = f64_engine(p, form, h.engine);
     if (form == KMX_FORM_DIGITS) {
       e = cudaErrorNotSupported;
@@ -596,6 +604,37 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
   MixedArrays ma;
   cudaError_t e = mixed_prepare(count, dims, nullptr, classes, nclasses, ws, need, status, s, &ma);
   if (e != cudaSuccess) return cuda_fail(e);
+  if (o.engine == KMX_ENGINE_PERSISTENT && sizeof(T) == 8 && !det &&
+      (o.form == KMX_FORM_AUTO || o.form == KMX_FORM_SPLIT)) {
+    // one persistent launch over every class (generic double-float kernel)
+    long long maxN = 1;
+    for (int c = 0; c < nclasses; ++c) {
+      long long N = 0;
+      ipow_checked(classes[2 * c + 1], classes[2 * c], &N);
+      if (N > maxN) maxN = N;
+    }
+    Problem p;
+    base_square(p, L_MIXED, 1, 2, 2, 2);
+    p.count = count;
+    p.order = ma.order;
+    p.a_off = a_off;
+    p.A = Aarray;
+    p.X = pX;
+    p.Y = const_cast<T**>(pY);
+    p.trans = o.transpose;
+    p.status = status;
+    rc = redo_ptr(&p.redo_ctr);
+    if (rc != KMX_OK) return rc;
+    if (W && Wcap > 0) {
+      p.Wbase = W;
+      p.w_stride = 2 * maxN;
+      const size_t slots = Wcap / (2 * (size_t)maxN * sizeof(T));
+      p.nslots = (int)(slots < (size_t)count ? slots : (size_t)count);
+    }
+    e = launch_mixed_persistent(p, dims, ma.queue, maxN, s);
+    if (e == cudaErrorInvalidValue) return KMX_ERR_WORKSPACE;
+    return e == cudaSuccess ? KMX_OK : cuda_fail(e);
+  }
   SegArrays sa{};
   if (det) {
     long long yb[KMX_MAX_CLASSES];

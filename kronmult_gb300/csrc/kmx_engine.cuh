@@ -1006,6 +1006,196 @@ struct DfRows {
   }
 };
 
+// One entry of the generic double-float kernel (shape from p, which may be
+// a per-entry copy): scales, split, the d modes, the cancellation guard.
+// gbase: the group's shared memory (factors, exponents); w0/w1: its buffers
+// (shared memory, or the global workspace); two: both buffers usable.
+template <int R>
+__device__ __forceinline__ void gen_split_entry(const Problem& p, const EntryPtrs<double>& en,
+                                                unsigned char* gbase, double* w0, double* w1,
+                                                int* sExp, float* sNrm, bool two, int lt, int G,
+                                                int g) {
+  const int d = p.d;
+  int aoff[MAXD + 1];
+  aoff[0] = 0;
+#pragma unroll
+  for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
+  df* sA = reinterpret_cast<df*>(gbase);
+  const bool excl = p.y_exclusive != 0;
+  const long long Nx = p.Nx;
+  // --- scales: max exponent field per factor and of X ---
+  if (lt < MAXD + 2) {
+    sExp[lt] = 0;
+    sNrm[lt] = 0.f;
+  }
+  group_sync(g, G);
+  for (int l = 0; l < d; ++l) {
+    const int ml = p.m[l], nl = p.n[l];
+    int em = 0;
+    for (int i = lt; i < ml * nl; i += G) {
+      const int a = i / nl, j = i - a * nl;
+      em = max(em, exp_field(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                     : en.A[l][a + (long long)j * en.ld[l]]));
+    }
+    em = __reduce_max_sync(0xffffffffu, em);  // one shared atomic per warp
+    if ((lt & 31) == 0 && em > 0) atomicMax(&sExp[l], em);
+  }
+  {
+    int ex = 0;
+    for (long long i = lt; i < Nx; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
+    ex = __reduce_max_sync(0xffffffffu, ex);
+    if ((lt & 31) == 0 && ex > 0) atomicMax(&sExp[MAXD], ex);
+  }
+  group_sync(g, G);
+  int nonfinite = (sExp[MAXD] == 2047);
+  int escale = sExp[MAXD] - 1023;
+  bool anyzero = sExp[MAXD] == 0;
+  for (int l = 0; l < d; ++l) {
+    nonfinite |= (sExp[l] == 2047);
+    escale += sExp[l] - 1023;
+    anyzero = anyzero || sExp[l] == 0;
+  }
+  if (nonfinite) {
+    // Inf/NaN propagate exactly as in FP64 (0 * Inf included): the plain
+    // entry on the same memory
+    gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
+    group_sync(g, G);
+    return;
+  }
+  if (anyzero) {  // kron(...) X is exactly zero
+    group_sync(g, G);
+    return;
+  }
+  // --- factors (transposed: sA[aoff[l] + j*m_l + a] = A_l(a, j)) and X, split ---
+  for (int l = 0; l < d; ++l) {
+    const int ml = p.m[l], nl = p.n[l];
+    float an = 0.f;
+    for (int i = lt; i < ml * nl; i += G) {
+      const int j = i / ml, a = i - j * ml;
+      const df s = split_scaled(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
+                                        : en.A[l][a + (long long)j * en.ld[l]],
+                                sExp[l]);
+      sA[aoff[l] + i] = s;
+      an = __fmaf_rn(s.hi, s.hi, an);
+    }
+    an = warp_sum(an);
+    if ((lt & 31) == 0) atomicAdd(&sNrm[l], an);
+  }
+  df* b0 = reinterpret_cast<df*>(w0);
+  df* b1 = reinterpret_cast<df*>(w1);
+  const int ex = sExp[MAXD];
+  float gsum = 0.f;  // guard: this thread's part of ||X||^2, then of ||KX||^2
+  for (long long i = lt; i < Nx; i += G) {
+    const df s = split_scaled(__ldg(en.X + i), ex);
+    b0[i] = s;
+    gsum = __fmaf_rn(s.hi, s.hi, gsum);
+  }
+  gsum = warp_sum(gsum);
+  if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD], gsum);
+  gsum = 0.f;
+  group_sync(g, G);
+  // Out of place: a lane owns rows a0..a0+R-1 of one fiber of mode k.  The
+  // last mode (dst == nullptr) adds its outputs to Y, or subtracts them (neg).
+  auto out_of_place = [&](int k, unsigned outer, const df* src, df* dst, bool neg) {
+    unsigned s = 1;
+    for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
+    const int mk = p.m[k], nk = p.n[k];
+    const df* At = sA + aoff[k];
+    const int nb = (mk + R - 1) / R;
+    const FastDiv fs(s), fb((unsigned)nb);
+    const unsigned total = outer * (unsigned)nb * s;
+    for (unsigned q = lt; q < total; q += G) {
+      const unsigned t = fs(q);
+      const unsigned rr = q - t * s;
+      const unsigned o = fb(t);
+      const int a0 = (int)(t - o * (unsigned)nb) * R;
+      const df* v = src + (long long)o * nk * s + rr;
+      df av[R];
+      DfRows<R> acc;
+#pragma unroll
+      for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
+      acc.first(av, v[0]);
+      for (int j = 1; j < nk; ++j) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
+        acc.add(av, v[(long long)j * s]);
+      }
+      const long long obase_q = ((long long)o * mk + a0) * s + rr;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (a0 + r < mk) {
+          const df o2 = acc.get(r);
+          if (dst == nullptr) {
+            if (!neg) gsum = __fmaf_rn(o2.hi, o2.hi, gsum);
+            const double y =
+                f32_to_f64_scaled(o2.hi, escale) + f32_to_f64_scaled(o2.lo, escale);
+            y_accumulate(en.Y + obase_q + (long long)r * s, neg ? -y : y, excl);
+          } else {
+            dst[obase_q + (long long)r * s] = o2;
+          }
+        }
+      }
+    }
+  };
+  df* cur = b0;
+  unsigned outer = 1, outer_last = 1;
+  for (int k = 0; k < d; ++k) {
+    unsigned s = 1;
+    for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
+    const int mk = p.m[k], nk = p.n[k];
+    const df* At = sA + aoff[k];
+    const bool last = (k == d - 1);
+    const int nb = (mk + R - 1) / R;
+    if (!last && !two && gen_split_in_place(mk, nk)) {
+      // one buffer: in place on cur, one fiber per lane
+      const FastDiv fs(s);
+      const unsigned F = outer * s;
+      for (unsigned f = lt; f < F; f += G) {
+        const unsigned o = fs(f);
+        const unsigned r0 = f - o * s;
+        df* base = cur + (long long)o * nk * s + r0;
+        df v[GEN_SPLIT_MAXN];
+        for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
+        for (int ab = 0; ab < nb; ++ab) {
+          const int a0 = ab * R;
+          df av[R];
+          DfRows<R> acc;
+#pragma unroll
+          for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
+          acc.first(av, v[0]);
+          for (int j = 1; j < nk; ++j) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
+            acc.add(av, v[j]);
+          }
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (a0 + r < mk) base[(long long)(a0 + r) * s] = acc.get(r);
+        }
+      }
+    } else {
+      df* dst = last ? nullptr : (cur == b0 ? b1 : b0);
+      if (last) outer_last = outer;
+      out_of_place(k, outer, cur, dst, false);
+      if (!last) cur = dst;
+    }
+    group_sync(g, G);
+    outer *= (unsigned)mk;
+  }
+  gsum = warp_sum(gsum);
+  if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD + 1], gsum);
+  group_sync(g, G);
+  // cancellation guard (uniform over the group): take the contribution back
+  // (the last mode leaves its input unchanged, the same arithmetic gives the
+  // same values) and add the plain FP64 result instead
+  if (!p.guard_off && guard_fails(sNrm[MAXD + 1], sNrm[MAXD], sNrm, d, Nx)) {
+    out_of_place(d - 1, outer_last, cur, nullptr, true);
+    group_sync(g, G);
+    gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
+    if (lt == 0) count_redo(p.redo_ctr, 0);
+  }
+}
+
 template <bool GBUF, int R>
 __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1020,7 +1210,6 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
 #pragma unroll
   for (int l = 0; l < MAXD; ++l) aoff[l + 1] = aoff[l] + (l < d ? p.m[l] * p.n[l] : 0);
   unsigned char* gbase = smem + (size_t)g * p.group_smem;
-  df* sA = reinterpret_cast<df*>(gbase);
   const size_t fac_bytes = ((size_t)aoff[d] * 8 + 15) / 16 * 16;
   int* sExp = reinterpret_cast<int*>(gbase + fac_bytes);  // MAXD + 2 ints
   float* sNrm0 = reinterpret_cast<float*>(sExp + MAXD + 2);  // [2][MAXD + 2] guard sums
@@ -1029,8 +1218,6 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
   const bool two = GBUF || (size_t)p.group_smem >= fac_bytes + GEN_SPLIT_HDR + 2 * bbytes;
   const long long slot0 = (long long)blockIdx.x * E + g;
   const long long step = (long long)gridDim.x * E;
-  const bool excl = p.y_exclusive != 0;
-  const long long Nx = p.Nx;
   int par = 0;  // guard sums alternate between two slots (entry parity)
   EntryStream es(p, slot0, step);
   for (long long entry; es.next(p, entry);) {
@@ -1048,177 +1235,7 @@ __global__ void __launch_bounds__(MAX_THREADS) gen_split_kernel(const Problem p)
         continue;
       }
     }
-    // --- scales: max exponent field per factor and of X ---
-    if (lt < MAXD + 2) {
-      sExp[lt] = 0;
-      sNrm[lt] = 0.f;
-    }
-    group_sync(g, G);
-    for (int l = 0; l < d; ++l) {
-      const int ml = p.m[l], nl = p.n[l];
-      int em = 0;
-      for (int i = lt; i < ml * nl; i += G) {
-        const int a = i / nl, j = i - a * nl;
-        em = max(em, exp_field(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
-                                       : en.A[l][a + (long long)j * en.ld[l]]));
-      }
-      em = __reduce_max_sync(0xffffffffu, em);  // one shared atomic per warp
-      if ((lt & 31) == 0 && em > 0) atomicMax(&sExp[l], em);
-    }
-    {
-      int ex = 0;
-      for (long long i = lt; i < Nx; i += G) ex = max(ex, exp_field(__ldg(en.X + i)));
-      ex = __reduce_max_sync(0xffffffffu, ex);
-      if ((lt & 31) == 0 && ex > 0) atomicMax(&sExp[MAXD], ex);
-    }
-    group_sync(g, G);
-    int nonfinite = (sExp[MAXD] == 2047);
-    int escale = sExp[MAXD] - 1023;
-    bool anyzero = sExp[MAXD] == 0;
-    for (int l = 0; l < d; ++l) {
-      nonfinite |= (sExp[l] == 2047);
-      escale += sExp[l] - 1023;
-      anyzero = anyzero || sExp[l] == 0;
-    }
-    if (nonfinite) {
-      // Inf/NaN propagate exactly as in FP64 (0 * Inf included): the plain
-      // entry on the same memory
-      gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
-      group_sync(g, G);
-      continue;
-    }
-    if (anyzero) {  // kron(...) X is exactly zero
-      group_sync(g, G);
-      continue;
-    }
-    // --- factors (transposed: sA[aoff[l] + j*m_l + a] = A_l(a, j)) and X, split ---
-    for (int l = 0; l < d; ++l) {
-      const int ml = p.m[l], nl = p.n[l];
-      float an = 0.f;
-      for (int i = lt; i < ml * nl; i += G) {
-        const int j = i / ml, a = i - j * ml;
-        const df s = split_scaled(p.trans ? en.A[l][j + (long long)a * en.ld[l]]
-                                          : en.A[l][a + (long long)j * en.ld[l]],
-                                  sExp[l]);
-        sA[aoff[l] + i] = s;
-        an = __fmaf_rn(s.hi, s.hi, an);
-      }
-      an = warp_sum(an);
-      if ((lt & 31) == 0) atomicAdd(&sNrm[l], an);
-    }
-    df* b0 = reinterpret_cast<df*>(w0);
-    df* b1 = reinterpret_cast<df*>(w1);
-    const int ex = sExp[MAXD];
-    float gsum = 0.f;  // guard: this thread's part of ||X||^2, then of ||KX||^2
-    for (long long i = lt; i < Nx; i += G) {
-      const df s = split_scaled(__ldg(en.X + i), ex);
-      b0[i] = s;
-      gsum = __fmaf_rn(s.hi, s.hi, gsum);
-    }
-    gsum = warp_sum(gsum);
-    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD], gsum);
-    gsum = 0.f;
-    group_sync(g, G);
-    // Out of place: a lane owns rows a0..a0+R-1 of one fiber of mode k.  The
-    // last mode (dst == nullptr) adds its outputs to Y, or subtracts them (neg).
-    auto out_of_place = [&](int k, unsigned outer, const df* src, df* dst, bool neg) {
-      unsigned s = 1;
-      for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
-      const int mk = p.m[k], nk = p.n[k];
-      const df* At = sA + aoff[k];
-      const int nb = (mk + R - 1) / R;
-      const FastDiv fs(s), fb((unsigned)nb);
-      const unsigned total = outer * (unsigned)nb * s;
-      for (unsigned q = lt; q < total; q += G) {
-        const unsigned t = fs(q);
-        const unsigned rr = q - t * s;
-        const unsigned o = fb(t);
-        const int a0 = (int)(t - o * (unsigned)nb) * R;
-        const df* v = src + (long long)o * nk * s + rr;
-        df av[R];
-        DfRows<R> acc;
-#pragma unroll
-        for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
-        acc.first(av, v[0]);
-        for (int j = 1; j < nk; ++j) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
-          acc.add(av, v[(long long)j * s]);
-        }
-        const long long obase_q = ((long long)o * mk + a0) * s + rr;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          if (a0 + r < mk) {
-            const df o2 = acc.get(r);
-            if (dst == nullptr) {
-              if (!neg) gsum = __fmaf_rn(o2.hi, o2.hi, gsum);
-              const double y =
-                  f32_to_f64_scaled(o2.hi, escale) + f32_to_f64_scaled(o2.lo, escale);
-              y_accumulate(en.Y + obase_q + (long long)r * s, neg ? -y : y, excl);
-            } else {
-              dst[obase_q + (long long)r * s] = o2;
-            }
-          }
-        }
-      }
-    };
-    df* cur = b0;
-    unsigned outer = 1, outer_last = 1;
-    for (int k = 0; k < d; ++k) {
-      unsigned s = 1;
-      for (int l = k + 1; l < d; ++l) s *= (unsigned)p.n[l];
-      const int mk = p.m[k], nk = p.n[k];
-      const df* At = sA + aoff[k];
-      const bool last = (k == d - 1);
-      const int nb = (mk + R - 1) / R;
-      if (!last && !two && gen_split_in_place(mk, nk)) {
-        // one buffer: in place on cur, one fiber per lane
-        const FastDiv fs(s);
-        const unsigned F = outer * s;
-        for (unsigned f = lt; f < F; f += G) {
-          const unsigned o = fs(f);
-          const unsigned r0 = f - o * s;
-          df* base = cur + (long long)o * nk * s + r0;
-          df v[GEN_SPLIT_MAXN];
-          for (int j = 0; j < nk; ++j) v[j] = base[(long long)j * s];
-          for (int ab = 0; ab < nb; ++ab) {
-            const int a0 = ab * R;
-            df av[R];
-            DfRows<R> acc;
-#pragma unroll
-            for (int r = 0; r < R; ++r) av[r] = At[min(a0 + r, mk - 1)];
-            acc.first(av, v[0]);
-            for (int j = 1; j < nk; ++j) {
-#pragma unroll
-              for (int r = 0; r < R; ++r) av[r] = At[j * mk + min(a0 + r, mk - 1)];
-              acc.add(av, v[j]);
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r)
-              if (a0 + r < mk) base[(long long)(a0 + r) * s] = acc.get(r);
-          }
-        }
-      } else {
-        df* dst = last ? nullptr : (cur == b0 ? b1 : b0);
-        if (last) outer_last = outer;
-        out_of_place(k, outer, cur, dst, false);
-        if (!last) cur = dst;
-      }
-      group_sync(g, G);
-      outer *= (unsigned)mk;
-    }
-    gsum = warp_sum(gsum);
-    if ((lt & 31) == 0) atomicAdd(&sNrm[MAXD + 1], gsum);
-    group_sync(g, G);
-    // cancellation guard (uniform over the group): take the contribution back
-    // (the last mode leaves its input unchanged, the same arithmetic gives the
-    // same values) and add the plain FP64 result instead
-    if (!p.guard_off && guard_fails(sNrm[MAXD + 1], sNrm[MAXD], sNrm, d, Nx)) {
-      out_of_place(d - 1, outer_last, cur, nullptr, true);
-      group_sync(g, G);
-      gen_plain_entry<double>(p, en, reinterpret_cast<double*>(gbase), w0, w1, lt, G, g);
-      if (lt == 0) count_redo(p.redo_ctr, 0);
-    }
+    gen_split_entry<R>(p, en, gbase, w0, w1, sExp, sNrm, two, lt, G, g);
   }
 }
 

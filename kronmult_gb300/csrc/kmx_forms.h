@@ -12,6 +12,10 @@ cudaError_t launch_f32_plain(Problem& p, const LaunchHint& h, cudaStream_t s);
 // shared memory), decided as the launchers decide (seg: deterministic mode).
 bool needs_workspace_f64_plain(const Problem& p, bool seg, int engine);
 bool needs_workspace_f64_split(const Problem& p, bool seg, int engine);
+// One persistent launch over every instance of a mixed-shape FP64 call
+// (kmx_persist.cu): p.order = instances grouped by class, queue zeroed.
+cudaError_t launch_mixed_persistent(Problem& p, const int* dims, int* queue, long long max_elems,
+                                    cudaStream_t s);
 // The xbatched FP64 problem the C ABI would run for (d, n, lda) and the form
 // it would pick for `form` (KMX_FORM_*); KMX_OK or a kmx_status.
 int xbatched_f64_plan(int d, int n, int lda, int form, int accumulate, bool* needs_ws);

@@ -8,6 +8,7 @@
 #include <type_traits>
 #include <unordered_map>
 
+#include "kmx_cluster.cuh"
 #include "kmx_engine.cuh"
 #include "kmx_small.cuh"
 #include "kmx_tile.cuh"
@@ -267,6 +268,75 @@ inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHi
   return cudaLaunchKernel(k.func, dim3(grid), dim3(small::THREADS), args, k.smem, stream);
 }
 
+// ---------------------------------------------------------------------------
+// Cluster kernels (kmx_cluster.cuh): double-float entries beyond one SM's
+// shared memory, n CTAs per (entry, i1) sharing mode 2 through distributed
+// shared memory.
+// ---------------------------------------------------------------------------
+struct ClusterKernel {
+  const void* func = nullptr;
+  int smem = 0;
+  int threads = 0;
+  int cluster = 0;
+};
+
+template <int NN, int D>
+ClusterKernel cluster_entry() {
+  ClusterKernel k;
+  if constexpr (clus::supported(NN, D)) {
+    k.func = reinterpret_cast<const void*>(&clus::cluster_kernel<NN, D>);
+    k.smem = clus::Layout<NN, D>::BYTES;
+    k.threads = clus::cta_threads(NN, D);
+    k.cluster = NN;
+  }
+  return k;
+}
+
+// The cluster kernel for (nn, d): the shapes whose entries exceed the
+// register-tiled kernel's shared memory.
+inline ClusterKernel pick_cluster(int nn, int d) {
+  switch (nn * 10 + d) {
+    case 85: return cluster_entry<8, 5>();
+    case 66: return cluster_entry<6, 6>();
+    case 76: return cluster_entry<7, 6>();
+    case 86: return cluster_entry<8, 6>();
+    default: return ClusterKernel();
+  }
+}
+
+inline cudaError_t launch_cluster(Problem& p, const ClusterKernel& k, const LaunchHint& hint,
+                                  cudaStream_t stream) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  err = ensure_smem(k.func, dev, k.smem);
+  if (err != cudaSuccess) return err;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)k.cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)k.cluster);
+  cfg.blockDim = dim3((unsigned)k.threads);
+  cfg.dynamicSmemBytes = (size_t)k.smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int active = 0;
+  err = cudaOccupancyMaxActiveClusters(&active, k.func, &cfg);
+  if (err != cudaSuccess) return err;
+  if (active < 1) return cudaErrorInvalidConfiguration;
+  const long long want = (long long)p.count * k.cluster;  // (entry, i1) items
+  long long nclusters = active;
+  if (hint.max_ctas > 0 && nclusters * k.cluster > hint.max_ctas)
+    nclusters = hint.max_ctas / k.cluster > 0 ? hint.max_ctas / k.cluster : 1;
+  if (nclusters > want) nclusters = want;
+  cfg.gridDim = dim3((unsigned)(nclusters * k.cluster));
+  void* args[] = {&p};
+  return cudaLaunchKernelExC(&cfg, k.func, args);
+}
+
 // Bytes of shared memory one group needs (on-chip intermediate included).
 template <typename T, int FORM>
 size_t sq_group_smem(const Problem& p, bool gbuf) {
@@ -322,6 +392,9 @@ bool needs_workspace(const Problem& p, bool seg, int engine) {
     if (seg && square && !p.seg_key && pick_tile<T, FORM, true>(nn, p.d).func) return false;
     if (!seg && square && engine != 1 && pick_tile<T, FORM>(nn, p.d).func) return false;
   }
+  if constexpr (FORM == FORM_SPLIT) {
+    if (!seg && square && pick_cluster(nn, p.d).func) return false;
+  }
   if constexpr (FORM == FORM_WIDE) {
     return false;
   } else {
@@ -363,9 +436,17 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
       const TileKernel tk = square && !p.seg_key ? pick_tile<T, FORM, true>(nn, p.d) : TileKernel();
       if (tk.func) return launch_tile(p, tk, hint, stream);
     }
-    if (!seg && square && hint.engine != 1) {
-      const TileKernel tk = pick_tile<T, FORM>(nn, p.d);
+    if (!seg && square) {
+      const TileKernel tk = hint.engine != 1 ? pick_tile<T, FORM>(nn, p.d) : TileKernel();
       if (tk.func) return launch_tile(p, tk, hint, stream);
+      if constexpr (FORM == FORM_SPLIT) {
+        // entries beyond one SM's shared memory: a cluster per (entry, i1)
+        // when no workspace is given (or the cluster engine is asked for);
+        // with a workspace the per-mode kernels below run faster
+        const bool no_ws = p.wmode == 0 || p.nslots <= 0;
+        const ClusterKernel ck = (no_ws || hint.engine == 5) ? pick_cluster(nn, p.d) : ClusterKernel();
+        if (ck.func) return launch_cluster(p, ck, hint, stream);
+      }
     }
   }
   if constexpr (FORM == FORM_WIDE) {

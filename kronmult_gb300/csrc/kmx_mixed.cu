@@ -76,7 +76,7 @@ __global__ void class_range_kernel(const int* sorted_keys, int count, int nclass
 inline size_t al256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct MixLayout {
-  size_t keys, ids, skeys, order, offsets, counts, temp, temp_bytes, total;
+  size_t keys, ids, skeys, order, offsets, counts, queue, temp, temp_bytes, total;
 };
 
 MixLayout mix_layout(int count) {
@@ -94,6 +94,7 @@ MixLayout mix_layout(int count) {
   L.order = take(c * 4);
   L.offsets = take(KMX_MAX_CLASSES * 4);
   L.counts = take(KMX_MAX_CLASSES * 4);
+  L.queue = take(4);
   size_t t = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, t, (int*)nullptr, (int*)nullptr, (int*)nullptr,
                                   (int*)nullptr, (int)c);
@@ -141,6 +142,10 @@ cudaError_t mixed_prepare(int count, const int* dims, const int* cls, const int*
   class_range_kernel<<<1, KMX_MAX_CLASSES + 1, 0, s>>>(skeys, count, nclasses, offsets, counts);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  int* queue = reinterpret_cast<int*>(w + L.queue);
+  e = cudaMemsetAsync(queue, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  out->queue = queue;
   out->keys = keys;
   out->order = order;
   out->offsets = offsets;

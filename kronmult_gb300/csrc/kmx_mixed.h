@@ -12,6 +12,7 @@ struct MixedArrays {
   const int* order;    // instance ids sorted by class (stable)
   const int* offsets;  // first position of class c in order[] (device)
   const int* counts;   // instances of class c (device)
+  int* queue;          // work-queue counter of a persistent launch, zeroed on the stream
 };
 
 size_t mixed_workspace_bytes(int count);

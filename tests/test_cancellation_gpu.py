@@ -18,8 +18,10 @@ Bounds asserted per entry, with rho and the errors measured here:
   hands those entries to the guarded double-float pass.  The device counters
   (kmx_read_redo_counters) must show exactly those entries.
 Shapes cover every double-float kernel: register-tiled (6,4), (3,16); per-mode
-square (2,8); per-mode with the intermediate in the workspace (5,8); generic
-(3,10).  Every call goes through the C ABI."""
+square (2,8), and (5,8) with its intermediate in the workspace; the cluster
+kernel for (5,8) (engine "cluster"), whose guard decides per block of n^(d-2)
+outputs and counts blocks; generic (3,10).
+Every call goes through the C ABI."""
 import numpy as np
 import pytest
 
@@ -29,8 +31,10 @@ torch = pytest.importorskip("torch")
 
 EPS = [None, 1e-1, 1e-2, 1e-3, 1e-4, 1e-6, 1e-8]
 SHAPES = [(6, 4), (3, 16), (2, 8), (5, 8), (3, 10)]
+CLUSTER = {(5, 8)}  # shapes with a cluster kernel (form "cluster" below)
 U47 = 2.0 ** -47
-C_BOUND = {"plain": 0.02, "split_raw": 1.0, "split": 1.0, "auto": 1.0, "digits": 1.0}
+C_BOUND = {"plain": 0.02, "split_raw": 1.0, "split": 1.0, "auto": 1.0, "digits": 1.0,
+           "cluster": 1.0}
 TOL = 1e-13
 
 
@@ -57,12 +61,15 @@ def _batch(d, n):
 
 
 def _run(kmx, d, n, A, X, form):
+    """form "cluster": the split form on the cluster kernel."""
     At = torch.from_numpy(A).cuda()
     Xt = torch.from_numpy(X).cuda()
     Y = torch.zeros_like(Xt)
     W = torch.empty_like(Xt)  # workspace for entries beyond shared memory
     kmx.read_redo_counters()
-    kmx.kronmult_batched(d, n, At, Xt, Y, W, A.shape[0], form=form)
+    engine = "cluster" if form == "cluster" else None
+    kmx.kronmult_batched(d, n, At, Xt, Y, W, A.shape[0], form="split" if form == "cluster" else form,
+                         engine=engine)
     torch.cuda.synchronize()
     assert kmx.check_device_status() == 0
     return Y.cpu().numpy(), kmx.read_redo_counters()
@@ -89,7 +96,8 @@ def test_cancellation_sweep(kmx, oracle, d, n):
         fired = rho_f < 0.25
         borderline = np.any((rho_f > 0.2) & (rho_f < 0.3))
         errs = {}
-        for form in ("plain", "split_raw", "split", "auto", "digits"):
+        forms = ("plain", "split_raw", "split", "auto", "digits")
+        for form in forms + (("cluster",) if (d, n) in CLUSTER else ()):
             y, (guard, handback) = _run(kmx, d, n, A, X, form)
             err = (np.linalg.norm((y - Yx).astype(np.float64), axis=1) / ynorm)
             errs[form] = float(err.max())
@@ -97,6 +105,8 @@ def test_cancellation_sweep(kmx, oracle, d, n):
             assert np.all(err <= bound), (form, eps, float(np.max(err / bound)))
             if form in ("split", "auto") and not borderline:
                 assert guard == int(fired.sum()), (form, eps, guard, int(fired.sum()))
+            if form == "cluster" and not borderline:  # one count per block, n*n per entry
+                assert guard == int(fired.sum()) * n * n, (form, eps, guard)
             if form in ("plain", "split_raw"):
                 assert guard == 0
             if form == "digits" and (d, n) in ((6, 4), (3, 16)) and not borderline:
@@ -105,8 +115,8 @@ def test_cancellation_sweep(kmx, oracle, d, n):
                 assert handback >= int(fired.sum()), (eps, handback)
                 assert guard == int(fired.sum()), (eps, guard)
         if errs["plain"] <= TOL:
-            for form in ("split", "auto", "digits"):
-                assert errs[form] <= TOL, (form, eps, errs)
+            for form in ("split", "auto", "digits", "cluster"):
+                assert errs.get(form, 0.0) <= TOL, (form, eps, errs)
         report.append((eps, float(np.median(rho)), errs))
     # the unguarded double-float form really does lose accuracy where plain
     # FP64 does not (else the sweep would not exercise the guard)

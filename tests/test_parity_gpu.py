@@ -590,6 +590,26 @@ def test_mixed_shapes_one_call(kmx, oracle, form):
     check_status(kmx)
 
 
+@pytest.mark.parametrize("form", ["auto", "split"])
+def test_mixed_shapes_persistent_engine(kmx, oracle, form):
+    """KMX_ENGINE_PERSISTENT: one launch over every class, instances popped
+    from a device work queue, each run by the generic double-float kernel with
+    its own (d, n) -- on chip or, for the 8^6 entries, in the workspace."""
+    c = _mixed_case(kmx, 44, 300)
+    ybuf = c["ybuf"].clone()
+    pY = kmx.pointer_array(ybuf, c["xoffs"])
+    W = torch.empty(8 * 2 * 8 ** 6, dtype=torch.float64, device="cuda")  # 8 slots for 8^6 entries
+    kmx.read_redo_counters()
+    kmx.kronmult_mixed(dev(c["dims"]), c["pA"], dev(c["a_off"].astype(np.int64)), c["pX"], pY,
+                       c["classes"], W, form=form, engine="persistent")
+    y = host(ybuf)
+    ref = _mixed_reference(oracle, c)
+    for i, r in enumerate(ref):
+        seg = y[c["xoffs"][i]: c["xoffs"][i] + r.size]
+        assert blockwise_rel_err(seg, r) <= F64_TOL, (i, c["dims"][i])
+    check_status(kmx)
+
+
 def test_mixed_unknown_class_is_flagged(kmx):
     c = _mixed_case(kmx, 42, 20, ns=(2, 3), dmax=3)
     ybuf = c["ybuf"].clone()
