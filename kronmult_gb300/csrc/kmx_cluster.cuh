@@ -250,19 +250,22 @@ __global__ void __launch_bounds__(cta_threads(NN, D)) cluster_kernel(const Probl
 #pragma unroll
     for (int f = 0; f < FPT; ++f) {
       const int idx = lt + f * G;
-      if (idx < D * NN2) {
+      const bool own = idx < D * NN2;
+      float sq = 0.f;  // sNrm[0], [1]: rows i1 of A1 and r of A2 only
+      if (own) {
         const df s = tile::SplitPolicy::make(af[f], sExp[al[f]]);
         Pol::template store_factor<NN>(sA, idx, s);
         if (al[f] == 0 && ar[f] == i1) {
           sRow1[ac[f]] = s;
-          atomicAdd(&sNrm[0], s.hi * s.hi);
+          sq = s.hi * s.hi;
         } else if (al[f] == 1 && ar[f] == (int)r) {
           sRow2[ac[f]] = s;
-          atomicAdd(&sNrm[1], s.hi * s.hi);
+          sq = s.hi * s.hi;
         } else if (al[f] >= 2) {
-          atomicAdd(&sNrm[al[f]], s.hi * s.hi);
+          sq = s.hi * s.hi;
         }
       }
+      warp_run_add(sNrm, own ? al[f] : 0, sq, own);
     }
     cluster_sync();  // #1: every CTA's slice exponent published
     if (lt == 0) {

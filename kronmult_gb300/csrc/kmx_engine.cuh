@@ -125,6 +125,28 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// sums[key] += v for every lane of the warp whose `valid` is set, where key
+// does not decrease with the lane index (invalid lanes last): each run of
+// equal keys is summed by shuffles and its first lane adds the run's sum with
+// one shared-memory atomic, so no two lanes of a warp add to one address (a
+// factor's n*n squared entries otherwise queue on one word).  Every lane of
+// the warp calls it.
+__device__ __forceinline__ void warp_run_add(float* sums, int key, float v, bool valid) {
+  const int lane = threadIdx.x & 31;
+  if (!valid) {
+    key = 0x7fffffff;
+    v = 0.f;
+  }
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const float t = __shfl_down_sync(0xffffffffu, v, off);
+    const int tk = __shfl_down_sync(0xffffffffu, key, off);
+    if (lane + off < 32 && tk == key) v += t;
+  }
+  const int pk = __shfl_up_sync(0xffffffffu, key, 1);
+  if (valid && (lane == 0 || pk != key)) atomicAdd(&sums[key], v);
+}
+
 // true when the entry must be recomputed in FP64: out2 = ||KX||^2, x2 = ||X||^2,
 // a2[l] = ||A_l||_F^2 (all of scaled values), N = length of X (for m_l x n_l
 // factors E||A v||^2 = ||A||_F^2 ||v||^2 / n_l, so prod n_l is the normaliser)
@@ -729,14 +751,22 @@ __global__ void __launch_bounds__(MAX_THREADS, (GBUF && NN <= 8) ? 2 : 0) sq_spl
       group_sync(g, G);
       continue;
     }
-    // --- factors, scaled and split ---
-    for (int i = lt; i < d * NN2; i += G) {
-      const int l = i / NN2, r = i - l * NN2, a = r / NN, j = r - a * NN;
-      const double* Al = en.A[l];
-      const double v = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
-      const df s = split_scaled(v, sExp[l]);
-      sA[i] = s;
-      atomicAdd(&sNrm[l], s.hi * s.hi);
+    // --- factors, scaled and split (warp-uniform trip count: the norm
+    // sums run over whole warps) ---
+    for (int i0 = 0; i0 < d * NN2; i0 += G) {
+      const int i = i0 + lt;
+      const bool own = i < d * NN2;
+      const int l = own ? i / NN2 : 0;
+      float sq = 0.f;
+      if (own) {
+        const int r = i - l * NN2, a = r / NN, j = r - a * NN;
+        const double* Al = en.A[l];
+        const double v = p.trans ? Al[j + (long long)a * en.ld[l]] : Al[a + (long long)j * en.ld[l]];
+        const df s = split_scaled(v, sExp[l]);
+        sA[i] = s;
+        sq = s.hi * s.hi;
+      }
+      warp_run_add(sNrm, l, sq, own);
     }
     const int ex = sExp[MAXD];
     group_sync(g, G);

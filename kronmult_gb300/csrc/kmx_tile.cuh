@@ -194,8 +194,8 @@ struct SplitPolicy : FlatFactors<df> {
 };
 
 // Double-float on packed FP32 pairs (kmx_pack.cuh): two output rows per
-// instruction.  Factors are stored as row pairs (high, low and negated high
-// parts); the arithmetic per value is that of SplitPolicy.
+// instruction.  Factors are stored as row pairs (high and low parts); the
+// arithmetic per value is that of SplitPolicy.
 struct PackedSplitPolicy : SplitPolicy {
   static constexpr bool PACKED = true;
   template <int NN>
@@ -211,10 +211,9 @@ struct PackedSplitPolicy : SplitPolicy {
     constexpr int NN2 = NN * NN;
     const int l = idx / NN2, r = (idx - l * NN2) / NN, j = idx - l * NN2 - r * NN;
     float* f = reinterpret_cast<float*>(base + (size_t)l * factor_bytes<NN>()) +
-               ((r >> 1) * NN + j) * 6 + (r & 1);
+               ((r >> 1) * NN + j) * 4 + (r & 1);
     f[0] = a.hi;
     f[2] = a.lo;
-    f[4] = -a.hi;
   }
 };
 
@@ -274,14 +273,15 @@ __device__ __forceinline__ void contract_tile_packed(df* v, const pk2::RowPair* 
     // first mode: columns (fixed second index), rows paired
 #pragma unroll
     for (int c = 0; c < NN; ++c) {
-      u64 vh[NN], vl[NN], oh[RP], ol[RP];
+      u64 vh[NN], vl[NN], nvh[NN], oh[RP], ol[RP];
 #pragma unroll
       for (int j = 0; j < NN; ++j) {
         vh[j] = pk2::bcast(v[j * NN + c].hi);
         vl[j] = pk2::bcast(v[j * NN + c].lo);
+        nvh[j] = pk2::bcast(-v[j * NN + c].hi);
       }
 #pragma unroll
-      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, nvh, oh[rp], ol[rp]);
 #pragma unroll
       for (int rp = 0; rp < RP; ++rp) {
         float h0, h1, l0, l1;
@@ -299,14 +299,15 @@ __device__ __forceinline__ void contract_tile_packed(df* v, const pk2::RowPair* 
     // second mode: rows (fixed first index), output columns paired
 #pragma unroll
     for (int r0 = 0; r0 < NN; ++r0) {
-      u64 vh[NN], vl[NN], oh[RP], ol[RP];
+      u64 vh[NN], vl[NN], nvh[NN], oh[RP], ol[RP];
 #pragma unroll
       for (int j = 0; j < NN; ++j) {
         vh[j] = pk2::bcast(v[r0 * NN + j].hi);
         vl[j] = pk2::bcast(v[r0 * NN + j].lo);
+        nvh[j] = pk2::bcast(-v[r0 * NN + j].hi);
       }
 #pragma unroll
-      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+      for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, nvh, oh[rp], ol[rp]);
 #pragma unroll
       for (int rp = 0; rp < RP; ++rp) {
         float h0, h1, l0, l1;
@@ -321,14 +322,15 @@ __device__ __forceinline__ void contract_tile_packed(df* v, const pk2::RowPair* 
       }
     }
   } else {
-    u64 vh[NN], vl[NN], oh[RP], ol[RP];
+    u64 vh[NN], vl[NN], nvh[NN], oh[RP], ol[RP];
 #pragma unroll
     for (int j = 0; j < NN; ++j) {
       vh[j] = pk2::bcast(v[j].hi);
       vl[j] = pk2::bcast(v[j].lo);
+      nvh[j] = pk2::bcast(-v[j].hi);
     }
 #pragma unroll
-    for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, oh[rp], ol[rp]);
+    for (int rp = 0; rp < RP; ++rp) pk2::dot_pair<NN>(A.pair(rp), vh, vl, nvh, oh[rp], ol[rp]);
 #pragma unroll
     for (int rp = 0; rp < RP; ++rp) {
       float h0, h1, l0, l1;
@@ -809,11 +811,13 @@ tile_kernel(const Problem p) {
     }
 #pragma unroll
     for (int f = 0; f < FPT; ++f) {
+      float sq = 0.f;
       if (fthr[f]) {
         const V a = Pol::make(af[f], Pol::SCALED ? ex_k[al[f]] : 0);
         Pol::template store_factor<NN>(sA, lt + f * G, a);
-        if constexpr (Pol::SCALED) atomicAdd(&nrm_k[al[f]], a.hi * a.hi);
+        if constexpr (Pol::SCALED) sq = a.hi * a.hi;
       }
+      if constexpr (Pol::SCALED) warp_run_add(nrm_k, al[f], sq, fthr[f]);
     }
     if (lt <= MAXD) ex_n[lt] = 0;
     if (lt == 0) {
