@@ -358,7 +358,7 @@ def run_ours(args):
 
     # e2e through the C ABI from pinned host buffers.  Every step copies its
     # inputs host->device and its result device->host; steps are pipelined
-    # over two device buffer sets and separate input, compute and output
+    # over three device buffer sets and separate input, compute and output
     # streams, so step k's kernel overlaps step k+1's input copies and step
     # k-1's result copy.
     e2e = None
@@ -377,9 +377,10 @@ def run_ours(args):
                 for _ in range(NB)]
         h2d = (Ah.numel() + Xh.numel() + Yh.numel()) * 8 + idx_h.numel() * 4
         d2h = Yh.numel() * 8
-        # the uploads and the download are split into NCH pieces on NCH streams
-        # each, so that several copy engines work at once
-        NCH = 4
+        # one upload and one download stream: splitting the copies over four
+        # streams each measured slower on GB300 (8.2 against 6.9 ms per step:
+        # the concurrent downloads slowed the kernel's step), two slower still
+        NCH = 1
         s_in = [torch.cuda.Stream() for _ in range(NCH)]
         s_cmp = torch.cuda.Stream()
         s_out = [torch.cuda.Stream() for _ in range(NCH)]
@@ -464,8 +465,8 @@ def run_ours(args):
                "device_ms_per_step": round(ms_e2e_dev, 3),
                "timing": f"host wall clock over {K2} steps, each step = H2D of pools and "
                          "index triples + device pointer build + C ABI call + D2H result; "
-                         "steps pipelined over three buffer sets, copies split over 4 streams "
-                         "each way; device_ms_per_step = the pointer build and kernel alone"}
+                         "steps pipelined over three buffer sets, one upload and one download "
+                         "stream; device_ms_per_step = the pointer build and kernel alone"}
 
     if rank != 0:
         if dist:
@@ -1005,6 +1006,9 @@ def run_rect(args):
                     kmx.pointer_array(X, [xoff[i] for i in idx]),
                     kmx.pointer_array(Y, [yoff[i] for i in idx])))
     one = lambda: kmx.kronmult_vmixed(dcls, pA, a_off, pX, pY, classes)  # noqa: E731
+    # one persistent launch over every class (device work queue)
+    pers = lambda: kmx.kronmult_vmixed(dcls, pA, a_off, pX, pY, classes,  # noqa: E731
+                                       engine="persistent")
 
     def separate():
         for d, m, n, b, qa, qx, qy in per:
@@ -1012,6 +1016,10 @@ def run_rect(args):
 
     ms_one = _events_time(torch, one, max(3, args.steps // 2), 2)
     ms_sep = _events_time(torch, separate, max(3, args.steps // 2), 2)
+    ms_pers = _events_time(torch, pers, max(3, args.steps // 2), 2)
+    Y.zero_()
+    pers()
+    Yp = Y.clone()
     Y.zero_()
     one()
     Y1 = Y.clone()
@@ -1022,8 +1030,11 @@ def run_rect(args):
              "one_call": {"gflops": round(fl / (ms_one * 1e-3) / 1e9, 1), "ms": round(ms_one, 3)},
              "per_shape_calls": {"gflops": round(fl / (ms_sep * 1e-3) / 1e9, 1),
                                  "ms": round(ms_sep, 3)},
-             "rel_err_one_vs_per_shape": float((Y1 - Y).norm() / Y.norm())}
-    del A, X, Y, Y1, pA, pX, pY, per
+             "persistent_one_launch": {"gflops": round(fl / (ms_pers * 1e-3) / 1e9, 1),
+                                       "ms": round(ms_pers, 3)},
+             "rel_err_one_vs_per_shape": float((Y1 - Y).norm() / Y.norm()),
+             "rel_err_persistent_vs_per_shape": float((Yp - Y).norm() / Y.norm())}
+    del A, X, Y, Y1, Yp, pA, pX, pY, per
     kmx.check_device_status()
     print(json.dumps({"metric": "kronmult GFLOP/s, shapes without a specialised kernel (FP64)",
                       "value": out[0]["forms"]["auto"]["gflops"], "unit": "GFLOP/s",

@@ -125,6 +125,15 @@ typedef struct kmx_options {
    * use and on growth), which calls on different streams must not share. */
   void* workspace;
   size_t workspace_bytes;
+  /* Launch shape; 0 takes the tuning table's choice for the call's (form,
+   * layout, d, n) with engine TUNED, else the built-in default.
+   * group_threads: threads per entry of the per-mode kernels (a multiple of
+   * 32, at most 512; the register-tiled and small-entry kernels fix their
+   * own); groups_per_cta: entries processed side by side in one CTA;
+   * ctas_per_sm: cap on the CTAs per SM the grid is sized for. */
+  int group_threads;
+  int groups_per_cta;
+  int ctas_per_sm;
 } kmx_options;
 
 /* ---------------------------------------------------------------------- */

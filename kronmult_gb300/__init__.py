@@ -104,28 +104,31 @@ def read_redo_counters(stream=None) -> tuple[int, int]:
     return int(c[0]), int(c[1])
 
 
-def _opt(form, accumulate, transpose, engine=None, workspace=None):
-    if form is None and accumulate is None and not transpose and engine is None:
+def _opt(form, accumulate, transpose, engine=None, workspace=None, launch=None):
+    if form is None and accumulate is None and not transpose and engine is None and not launch:
         return None
-    o = options(form or "auto", accumulate or "atomic", transpose, engine or "tuned")
+    o = options(form or "auto", accumulate or "atomic", transpose, engine or "tuned", launch)
     return C.byref(o)
 
 
 def kronmult_batched(d, n, A, X, Y, W=None, batchCount=None, *, form=None, accumulate=None,
-                     transpose=False, engine=None, stream=None):
-    """kronmult{d}_batched: A (n,n,d,batch) column-major, X/Y/W (n^d, batch)."""
+                     transpose=False, engine=None, launch=None, stream=None):
+    """kronmult{d}_batched: A (n,n,d,batch) column-major, X/Y/W (n^d, batch).
+    launch: (group_threads, groups_per_cta, ctas_per_sm) overrides, 0 = tuned."""
     f64 = _is_f64(A.dtype)
     b = batchCount if batchCount is not None else X.numel() // (n ** d)
     s = C.c_void_p(_stream(stream))
     L = lib()
     if f64:
         rc = L.kmx_kronmult_batched_f64_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
-                                           _opt(form, accumulate, transpose, engine), s)
+                                           _opt(form, accumulate, transpose, engine,
+                                                launch=launch), s)
     else:
         if form not in (None, "auto", "plain", "split", "tf32x3"):
             raise KmxError(4, "kmx_kronmult_batched_f32")
         rc = L.kmx_kronmult_batched_f32_ex(d, n, _addr(A), _addr(X), _addr(Y), _addr(W), b,
-                                           _opt(form, accumulate, transpose, engine), s)
+                                           _opt(form, accumulate, transpose, engine,
+                                                launch=launch), s)
     check(rc, f"kronmult{d}_batched")
 
 
@@ -147,7 +150,7 @@ def kronmult_pbatched(d, n, A, pX, pY, pW=None, batchCount=None, *, form=None, a
 
 def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subbatchCount=0, *,
                       dtype=None, form=None, accumulate=None, transpose=False, engine=None,
-                      stream=None):
+                      launch=None, stream=None):
     """kronmult{d}_xbatched: Aarray (d, batch) factor addresses with leading
     dimension lda; pX/pY/pW address arrays.  dtype is float64 unless given."""
     t = _torch()
@@ -158,11 +161,13 @@ def kronmult_xbatched(d, n, Aarray, lda, pX, pY, pW=None, batchCount=None, subba
     if f64:
         rc = L.kmx_kronmult_xbatched_f64_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
                                             _addr(pW), b, subbatchCount,
-                                            _opt(form, accumulate, transpose, engine), s)
+                                            _opt(form, accumulate, transpose, engine,
+                                                 launch=launch), s)
     else:
         rc = L.kmx_kronmult_xbatched_f32_ex(d, n, _addr(Aarray), lda, _addr(pX), _addr(pY),
                                             _addr(pW), b, subbatchCount,
-                                            _opt(form, accumulate, transpose, engine), s)
+                                            _opt(form, accumulate, transpose, engine,
+                                                 launch=launch), s)
     check(rc, f"kronmult{d}_xbatched")
 
 

@@ -44,7 +44,8 @@ class KmxError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("form", C.c_int), ("accumulate", C.c_int), ("transpose", C.c_int),
-                ("engine", C.c_int), ("workspace", C.c_void_p), ("workspace_bytes", C.c_size_t)]
+                ("engine", C.c_int), ("workspace", C.c_void_p), ("workspace_bytes", C.c_size_t),
+                ("group_threads", C.c_int), ("groups_per_cta", C.c_int), ("ctas_per_sm", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -153,8 +154,10 @@ def check(status: int, where: str) -> None:
 
 
 def options(form: str | int = "auto", accumulate: str | int = "atomic", transpose: bool = False,
-            engine: str | int = "tuned"):
+            engine: str | int = "tuned", launch=None):
+    """launch: (group_threads, groups_per_cta, ctas_per_sm), 0 = tuned/default."""
     f = FORMS[form] if isinstance(form, str) else int(form)
     a = ACCUMULATE[accumulate] if isinstance(accumulate, str) else int(accumulate)
     g = ENGINES[engine] if isinstance(engine, str) else int(engine)
-    return Options(f, a, 1 if transpose else 0, g, None, 0)
+    gt, ge, gs = (int(v) for v in launch) if launch else (0, 0, 0)
+    return Options(f, a, 1 if transpose else 0, g, None, 0, gt, ge, gs)

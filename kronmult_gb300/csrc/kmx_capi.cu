@@ -38,7 +38,7 @@ int* g_status_ptr[MAX_DEVICES];
 unsigned long long* g_redo_ptr[MAX_DEVICES];
 std::unordered_map<const void*, size_t> g_smem_set[MAX_DEVICES];
 
-kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0};
+kmx_options g_default = {KMX_FORM_AUTO, KMX_ACC_ATOMIC, 0, KMX_ENGINE_TUNED, nullptr, 0, 0, 0, 0};
 
 // Library-owned workspaces, stream ordered, one per device and purpose
 // (0: deterministic segments, 1: mixed-shape grouping, 2: digits-form redo list).
@@ -163,12 +163,33 @@ cudaError_t ensure_smem(const void* func, int dev, size_t bytes) {
   return e;
 }
 
-// Tuned engine for (form code, d, n): 0 when the table has no row.
-static int tuned_engine(int form, int d, int n) {
-  for (int i = 0; i < kTuneRows; ++i)
-    if (kTuneTable[i].form == form && kTuneTable[i].d == d && kTuneTable[i].n == n)
-      return kTuneTable[i].engine;
-  return 0;
+// Tuning-table row for (form code, layout class, d, n), layout class 0 for
+// the batched layout (disjoint Y blocks), 1 for the pointer layouts (Y blocks
+// may be shared, atomic accumulation); the other layout's row when the table
+// has none for this one; nullptr when it has neither.
+static const TuneRow* tuned_row(int form, int layout, int d, int n) {
+  const TuneRow* other = nullptr;
+  for (int i = 0; i < kTuneRows; ++i) {
+    const TuneRow& r = kTuneTable[i];
+    if (r.form != form || r.d != d || r.n != n) continue;
+    if (r.layout == layout) return &r;
+    other = &r;
+  }
+  return other;
+}
+
+static int layout_class(const Problem& p) { return p.layout == L_BATCHED ? 0 : 1; }
+
+// The launch hint of a TUNED call: the row's engine and launch shape where
+// the caller left them at 0.
+static void apply_tuned(LaunchHint& h, const Problem& p, int form, const kmx_options& o) {
+  if (!is_square(p)) return;
+  const TuneRow* r = tuned_row(form, layout_class(p), p.d, p.n[0]);
+  if (!r) return;
+  h.engine = r->engine;
+  if (o.group_threads == 0) h.group_threads = r->group_threads;
+  if (o.groups_per_cta == 0) h.groups_per_cta = r->groups_per_cta;
+  if (o.ctas_per_sm == 0) h.ctas_per_sm = r->ctas_per_sm;
 }
 
 // Tuned automatic FP64 form for (d, n): 0 when the table has no row.
@@ -192,10 +213,16 @@ static int resolve_f64_form(const Problem& p, int form) {
   return t ? t : (((sq && spec_n) || gen_split) ? KMX_FORM_SPLIT : KMX_FORM_PLAIN);
 }
 
+// Tuning-table form code of an FP64 form.
+static int f64_tune_form(int form) {
+  return (form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1;
+}
+
 // The tuned engine for an FP64 form on square shapes (0 = choose).
 static int f64_engine(const Problem& p, int form, int engine) {
   if (engine || !is_square(p)) return engine;
-  return tuned_engine((form == KMX_FORM_SPLIT || form == KMX_FORM_DIGITS) ? 2 : 1, p.d, p.n[0]);
+  const TuneRow* r = tuned_row(f64_tune_form(form), layout_class(p), p.d, p.n[0]);
+  return r ? r->engine : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -253,7 +280,10 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
     p.seg_queue = sa.queue;
     p.y_exclusive = 1;  // a segment's Y block belongs to one group
   }
-  LaunchHint h = {0, 0, 0, 0};
+  LaunchHint h = {};
+  h.group_threads = o.group_threads;
+  h.groups_per_cta = o.groups_per_cta;
+  h.ctas_per_sm = o.ctas_per_sm;
   static const int engine_env = [] {
     const char* e = std::getenv("KMX_ENGINE");
     return e ? std::atoi(e) : 0;
@@ -280,7 +310,7 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
       if (o.form == KMX_FORM_AUTO || o.form == KMX_FORM_SPLIT) {
         e = launch_f32_ref(p, h, s);
       } else if (o.form == KMX_FORM_PLAIN || o.form == KMX_FORM_TF32X3) {
-        if (h.engine == 0 && sq) h.engine = tuned_engine(3, p.d, p.n[0]);
+        if (h.engine == 0) apply_tuned(h, p, 3, o);
         e = launch_f32_plain(p, h, s);
       } else {
         return KMX_ERR_INVALID_ARG;
@@ -295,7 +325,7 @@ static int run_problem(Problem& p, bool is_f64, const kmx_options& o, cudaStream
         !(sq && form == KMX_FORM_SPLIT &&
           ((p.d == 5 && p.n[0] == 8) || (p.d == 6 && p.n[0] >= 6 && p.n[0] <= 8))))
       h.engine = 0;
-    h.engine = f64_engine(p, form, h.engine);
+    if (h.engine == 0) apply_tuned(h, p, f64_tune_form(form), o);
     if (form == KMX_FORM_DIGITS) {
       e = cudaErrorNotSupported;
       if (digits_supported(p)) {
@@ -539,6 +569,54 @@ static int xbatched_wide_impl(int in_type, int d, int n, const void* const* Aarr
   return run_problem(p, false, o, s, in_type);
 }
 
+// The persistent engine (kmx_persist.cu) for a mixed-shape call, FP64 only:
+// KMX_OK or an error, or PERSIST_SKIP when a class does not fit its kernel
+// (the caller then launches class by class).
+constexpr int PERSIST_SKIP = -1;
+
+static void persist_class(const Problem& q, PersistClass* c) {
+  c->d = q.d;
+  for (int l = 0; l < MAXD; ++l) {
+    c->m[l] = q.m[l];
+    c->n[l] = q.n[l];
+    c->ld[l] = q.ld[l];
+  }
+  c->Nx = q.Nx;
+  c->Ny = q.Ny;
+  c->sxw = q.sxw;
+}
+
+template <typename T>
+static int run_persistent(const PersistClasses& pc, int count, const MixedArrays& ma,
+                          const long long* a_off, const T* const* Aarray, T* const* pX,
+                          T* const* pY, T* W, size_t Wcap, const kmx_options& o, int* status,
+                          cudaStream_t s) {
+  long long ws_elems = 0;
+  if (!persistent_fits(pc, &ws_elems)) return PERSIST_SKIP;
+  Problem p;
+  base_square(p, L_MIXED, 1, 2, 2, 2);
+  p.count = count;
+  p.order = ma.order;
+  p.a_off = a_off;
+  p.A = Aarray;
+  p.X = pX;
+  p.Y = const_cast<T**>(pY);
+  p.trans = o.transpose;
+  p.status = status;
+  int rc = redo_ptr(&p.redo_ctr);
+  if (rc != KMX_OK) return rc;
+  if (ws_elems > 0 && W && Wcap > 0) {
+    p.Wbase = W;
+    p.w_stride = 2 * ws_elems;
+    const size_t slots = Wcap / (2 * (size_t)ws_elems * sizeof(T));
+    p.nslots = (int)(slots < (size_t)count ? slots : (size_t)count);
+  }
+  const cudaError_t e = launch_mixed_persistent(p, pc, ma.keys, ma.queue, s);
+  if (e == cudaErrorInvalidValue) return KMX_ERR_WORKSPACE;
+  if (e == cudaErrorNotSupported) return PERSIST_SKIP;
+  return e == cudaSuccess ? KMX_OK : cuda_fail(e);
+}
+
 // Deterministic mixed-shape calls: one set of segments over every instance,
 // Y blocks of ybytes[c] bytes for class c, handed to each class's launch
 // (which takes only its own entries, EntryStream).
@@ -606,34 +684,17 @@ static int mixed_impl(int count, const int* dims, const T* const* Aarray, const 
   if (e != cudaSuccess) return cuda_fail(e);
   if (o.engine == KMX_ENGINE_PERSISTENT && sizeof(T) == 8 && !det &&
       (o.form == KMX_FORM_AUTO || o.form == KMX_FORM_SPLIT)) {
-    // one persistent launch over every class (generic double-float kernel)
-    long long maxN = 1;
+    PersistClasses pc;
+    pc.count = nclasses;
     for (int c = 0; c < nclasses; ++c) {
+      Problem q;
       long long N = 0;
-      ipow_checked(classes[2 * c + 1], classes[2 * c], &N);
-      if (N > maxN) maxN = N;
+      ipow_checked(classes[2 * c + 1], classes[2 * c], &N);  // checked above
+      base_square(q, L_MIXED, classes[2 * c], classes[2 * c + 1], classes[2 * c + 1], N);
+      persist_class(q, &pc.c[c]);
     }
-    Problem p;
-    base_square(p, L_MIXED, 1, 2, 2, 2);
-    p.count = count;
-    p.order = ma.order;
-    p.a_off = a_off;
-    p.A = Aarray;
-    p.X = pX;
-    p.Y = const_cast<T**>(pY);
-    p.trans = o.transpose;
-    p.status = status;
-    rc = redo_ptr(&p.redo_ctr);
-    if (rc != KMX_OK) return rc;
-    if (W && Wcap > 0) {
-      p.Wbase = W;
-      p.w_stride = 2 * maxN;
-      const size_t slots = Wcap / (2 * (size_t)maxN * sizeof(T));
-      p.nslots = (int)(slots < (size_t)count ? slots : (size_t)count);
-    }
-    e = launch_mixed_persistent(p, dims, ma.queue, maxN, s);
-    if (e == cudaErrorInvalidValue) return KMX_ERR_WORKSPACE;
-    return e == cudaSuccess ? KMX_OK : cuda_fail(e);
+    rc = run_persistent(pc, count, ma, a_off, Aarray, pX, pY, W, Wcap, o, status, s);
+    if (rc != PERSIST_SKIP) return rc;
   }
   SegArrays sa{};
   if (det) {
@@ -709,6 +770,19 @@ static int vmixed_impl(int count, const int* cls, const T* const* Aarray, const 
   MixedArrays ma;
   cudaError_t e = mixed_prepare(count, nullptr, cls, nullptr, nclasses, ws, need, status, s, &ma);
   if (e != cudaSuccess) return cuda_fail(e);
+  if (o.engine == KMX_ENGINE_PERSISTENT && sizeof(T) == 8 && !det &&
+      (o.form == KMX_FORM_AUTO || o.form == KMX_FORM_SPLIT)) {
+    PersistClasses pc;
+    pc.count = nclasses;
+    for (int c = 0; c < nclasses; ++c) {
+      Problem q;
+      const int* r = classes + 13 * c;
+      rect_problem(q, L_MIXED, r[0], r + 1, r + 7, o);  // checked above
+      persist_class(q, &pc.c[c]);
+    }
+    rc = run_persistent(pc, count, ma, a_off, Aarray, pX, pY, W, Wcap, o, status, s);
+    if (rc != PERSIST_SKIP) return rc;
+  }
   SegArrays sa{};
   if (det) {
     long long yb[KMX_MAX_CLASSES];

@@ -22,10 +22,11 @@ enum Form : int { FORM_PLAIN = 1, FORM_SPLIT = 2, FORM_WIDE = 3, FORM_REF32 = 4 
 
 // Execution shape requested by the caller (0 = choose).
 struct LaunchHint {
-  int group_threads;
-  int groups_per_cta;
-  int max_ctas;  // cap on the grid (0 = fill the GPU)
-  int engine;    // 0 choose, 1 per-mode kernels, 2 register-tiled kernels, 3 small-entry kernels
+  int group_threads;   // per-mode kernels: threads per entry group (0 = default)
+  int groups_per_cta;  // entry groups per CTA (0 = default)
+  int max_ctas;        // cap on the grid (0 = fill the GPU)
+  int engine;          // 0 choose, 1 per-mode, 2 register-tiled, 3 small-entry, 5 cluster
+  int ctas_per_sm;     // cap on the resident CTAs per SM the grid is sized for (0 = occupancy)
 };
 
 struct DeviceInfo {
@@ -115,6 +116,7 @@ struct TileKernel {
   const void* func = nullptr;
   int group_threads = 0;
   int group_smem = 0;
+  int cta_threads = 0;  // the kernel's launch bound: groups_per_cta * group_threads <= this
 };
 
 template <typename T, int FORM, int NN, int D, bool SEG>
@@ -126,6 +128,7 @@ TileKernel tile_entry() {
     k.func = reinterpret_cast<const void*>(&tile::tile_kernel<Pol, NN, D, SEG>);
     k.group_threads = tile::group_threads(NN, D);
     k.group_smem = bytes;
+    k.cta_threads = tile::cta_threads(NN, D);
   }
   return k;
 }
@@ -168,6 +171,7 @@ inline cudaError_t launch_tile(Problem& p, const TileKernel& k, const LaunchHint
   const int G = k.group_threads;
   int E = hint.groups_per_cta > 0 ? hint.groups_per_cta : (G >= 256 ? 1 : 256 / G);
   while (E > 1 && (size_t)E * k.group_smem > (size_t)di.max_smem_optin) --E;
+  while (E > 1 && E * G > k.cta_threads) --E;
   if (E > p.count) E = p.count;
   const size_t smem = (size_t)E * k.group_smem;
   err = ensure_smem(k.func, dev, smem);
@@ -176,6 +180,7 @@ inline cudaError_t launch_tile(Problem& p, const TileKernel& k, const LaunchHint
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.func, E * G, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (hint.ctas_per_sm > 0 && per_sm > hint.ctas_per_sm) per_sm = hint.ctas_per_sm;
   const long long want = ((long long)p.count + E - 1) / E;
   long long cap = (long long)di.sms * per_sm;
   if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
@@ -260,6 +265,7 @@ inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHi
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.func, small::THREADS, k.smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (hint.ctas_per_sm > 0 && per_sm > hint.ctas_per_sm) per_sm = hint.ctas_per_sm;
   long long cap = (long long)di.sms * per_sm;
   if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
   // chunks of the launch: an upper bound when the count is on the device
@@ -513,6 +519,7 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, E * G, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) per_sm = 1;
+  if (hint.ctas_per_sm > 0 && per_sm > hint.ctas_per_sm) per_sm = hint.ctas_per_sm;
   long long want = ((long long)p.count + E - 1) / E;
   long long cap = (long long)di.sms * per_sm;
   if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;

@@ -79,7 +79,7 @@ extern "C" int kmx_kronmult_xbatched_f64_noalloc(int d, int n, const double* con
   void* scratch = nullptr;
   rc = noalloc_scratch(&scratch);
   if (rc != KMX_OK) return rc;
-  kmx_options o;
+  kmx_options o = {};  // launch shape and the rest: the defaults
   o.form = KMX_FORM_AUTO;
   o.accumulate = KMX_ACC_DETERMINISTIC;
   o.transpose = 0;

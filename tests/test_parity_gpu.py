@@ -610,6 +610,25 @@ def test_mixed_shapes_persistent_engine(kmx, oracle, form):
     check_status(kmx)
 
 
+def test_mixed_persistent_engine_large_n(kmx, oracle):
+    """Square classes the persistent kernel cannot apply in place (n > 16):
+    (3, 20) holds one buffer on chip but runs out of place, so it takes the
+    workspace; (2, 24) keeps two buffers on chip; (4, 3) is small."""
+    c = _mixed_case(kmx, 46, 60, ns=(20, 24, 3), dmax=4, cap=8000)
+    assert {(3, 20), (2, 24)} <= set(c["classes"])
+    ybuf = c["ybuf"].clone()
+    pY = kmx.pointer_array(ybuf, c["xoffs"])
+    W = torch.empty(16 * 2 * 8000, dtype=torch.float64, device="cuda")  # 16 slots
+    kmx.kronmult_mixed(dev(c["dims"]), c["pA"], dev(c["a_off"].astype(np.int64)), c["pX"], pY,
+                       c["classes"], W, engine="persistent")
+    y = host(ybuf)
+    ref = _mixed_reference(oracle, c)
+    for i, r in enumerate(ref):
+        seg = y[c["xoffs"][i]: c["xoffs"][i] + r.size]
+        assert blockwise_rel_err(seg, r) <= F64_TOL, (i, c["dims"][i])
+    check_status(kmx)
+
+
 def test_mixed_unknown_class_is_flagged(kmx):
     c = _mixed_case(kmx, 42, 20, ns=(2, 3), dmax=3)
     ybuf = c["ybuf"].clone()

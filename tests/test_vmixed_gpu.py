@@ -302,3 +302,38 @@ def test_vmixed_deterministic_vs_oracle(kmx, oracle, form):
     assert kmx.check_device_status() == 0
     assert np.array_equal(outs[0], outs[1])
     assert _err(outs[0], ref, cs, classes) <= F64_TOL
+
+
+@pytest.mark.parametrize("form", [None, "split"])
+def test_vmixed_persistent_engine(kmx, oracle, form):
+    """KMX_ENGINE_PERSISTENT on rectangular classes: one launch over every
+    class, instances from a device work queue, each run by the generic
+    double-float kernel with its own shape (two buffers on chip, or in the
+    caller's workspace for the class beyond shared memory)."""
+    cs = _case(15, CLASSES, 600, big_share=0.03)
+    ref = _oracle(oracle, CLASSES, cs)
+    dv = _device(kmx, cs, CLASSES)
+    kmx.kronmult_vmixed(dv["cls"], dv["pA"], dv["a_off"], dv["pX"], dv["pY"], CLASSES, dv["W"],
+                        form=form, engine="persistent")
+    torch.cuda.synchronize()
+    assert kmx.check_device_status() == 0
+    assert _err(dv["dY"].cpu().numpy(), ref, cs, CLASSES) <= F64_TOL
+
+
+def test_vmixed_persistent_unknown_class_is_flagged(kmx, oracle):
+    classes = CLASSES[:3]
+    cs = _case(16, classes, 60)
+    bad = 11
+    ref_cs = dict(cs)
+    ref_cs["cls"] = cs["cls"].copy()
+    ref_cs["cls"][bad] = 99
+    ref = _oracle(oracle, classes, ref_cs)
+    dv = _device(kmx, cs, classes)
+    dv["cls"][bad] = 99
+    kmx.kronmult_vmixed(dv["cls"], dv["pA"], dv["a_off"], dv["pX"], dv["pY"], classes, dv["W"],
+                        engine="persistent")
+    torch.cuda.synchronize()
+    with pytest.raises(kmx.KmxError):
+        kmx.check_device_status()
+    assert _err(dv["dY"].cpu().numpy(), ref, cs, classes) <= F64_TOL
+    assert kmx.check_device_status() == 0
