@@ -877,17 +877,17 @@ def run_kgemm(args):
 
 
 def run_big(args):
-    """Entries beyond one SM: batched FP64 d=6 n=8 (2 MB blocks, 256 entries)
-    and d=5 n=8 (256 KB blocks, 2048 entries), N(0,1)/sqrt(n) factors, N(0,1) X:
-    split and plain forms on the per-mode kernels with the intermediate in
-    the caller's workspace."""
+    """Entries beyond one SM: batched FP64 d=6 n=8 (2 MB blocks, 256 entries),
+    d=5 n=8 (256 KB, 2048), d=6 n=7 (0.9 MB, 512) and d=6 n=6 (0.37 MB, 1024),
+    N(0,1)/sqrt(n) factors, N(0,1) X: split and plain forms on the per-mode
+    kernels with the intermediate in the caller's workspace, and the split
+    form without a workspace (thread-block cluster kernels)."""
     import torch
 
     import kronmult_gb300 as kmx
 
     out = []
-    for d, batch in ((6, 256), (5, 2048)):
-        n = 8
+    for d, n, batch in ((6, 8, 256), (5, 8, 2048), (6, 7, 512), (6, 6, 1024)):
         N = n ** d
         g = torch.Generator(device="cuda").manual_seed(SEED + d)
         A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
@@ -896,8 +896,9 @@ def run_big(args):
         W = torch.zeros_like(X)
         fl = batch * 2.0 * d * n ** (d + 1)
         res = {}
-        for name, kw in (("split", dict(form="split")), ("plain", dict(form="plain"))):
-            call = lambda: kmx.kronmult_batched(d, n, A, X, Y, W, batch, **kw)
+        for name, kw, ws in (("split", dict(form="split"), W), ("plain", dict(form="plain"), W),
+                             ("split_cluster_no_workspace", dict(form="split"), None)):
+            call = lambda: kmx.kronmult_batched(d, n, A, X, Y, ws, batch, **kw)
             ms = _events_time(torch, call, max(3, args.steps // 2), 2)
             res[name] = {"gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3)}
         Yr = torch.zeros_like(X)
@@ -913,6 +914,56 @@ def run_big(args):
     print(json.dumps({"metric": "kronmult GFLOP/s, entries beyond one SM (FP64)",
                       "value": out[0]["forms"]["split"]["gflops"], "unit": "GFLOP/s",
                       "workload": "big", "cases": out, "data": "synthetic"}))
+
+
+def run_small(args):
+    """Small entries (the small-entry kernels' shapes): batched d=1 n=2, 4, 8,
+    d=2 n=4, 8, d=3 n=4, about 256 MiB of X per call, N(0,1)/2 factors,
+    N(0,1) X; FP64 plain and double-float, FP32 fused multiply-add; each with
+    the fraction of HBM its algorithmic bytes ((3N + d n^2) x element size per
+    entry) reach, and for FP64 plain the fraction of the FP64-pipe ceiling
+    max(flops / FP64 peak, bytes / HBM peak)."""
+    import ctypes as C
+
+    import torch
+
+    import kronmult_gb300 as kmx
+
+    peaks, peak_kind = load_peaks()
+    hbm = peaks["hbm_gbs"] * 1e9
+    r64 = C.c_double(0)
+    kmx.lib().kmx_probe_fma_rate(1, C.byref(r64))
+    fp64 = 2 * r64.value
+    out = []
+    for d, n in ((1, 2), (1, 4), (1, 8), (2, 4), (2, 8), (3, 4)):
+        N = n ** d
+        for form in ("plain", "split", "f32"):
+            dt = torch.float32 if form == "f32" else torch.float64
+            esz = 4 if form == "f32" else 8
+            batch = (256 << 20) // (N * esz)
+            g = torch.Generator(device="cuda").manual_seed(SEED + 10 * d + n)
+            A = torch.randn((batch, d, n, n), dtype=dt, device="cuda", generator=g) / 2
+            X = torch.randn((batch, N), dtype=dt, device="cuda", generator=g)
+            Y = torch.zeros_like(X)
+            f = "plain" if form == "f32" else form
+            call = lambda: kmx.kronmult_batched(d, n, A, X, Y, None, batch, form=f)
+            ms = _events_time(torch, call, max(3, args.steps // 2), 2)
+            fl = batch * 2.0 * d * n ** (d + 1)
+            by = batch * (3 * N + d * n * n) * esz
+            row = {"d": d, "n": n, "form": form, "batch": batch,
+                   "gflops": round(fl / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                   "hbm_frac": round(by / (ms * 1e-3) / hbm, 3)}
+            if form == "plain":
+                ceil = max(fl / fp64, by / hbm)
+                row["fp64_ceiling_frac"] = round(ceil / (ms * 1e-3), 3)
+            out.append(row)
+            del A, X, Y
+    kmx.check_device_status()
+    print(json.dumps({"metric": "HBM fraction of small entries (batched, tuned engine)",
+                      "value": out[0]["hbm_frac"], "unit": "fraction of measured HBM",
+                      "workload": "small", "hbm_peak_gbs": peaks["hbm_gbs"],
+                      "hbm_peak_source": peak_kind, "fp64_peak_tflops_measured": round(fp64 / 1e12, 3),
+                      "cases": out, "data": "synthetic"}))
 
 
 def run_rect(args):
@@ -1052,7 +1103,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload",
-                    choices=["xbatched", "mixed", "grad", "precision", "kgemm", "big", "rect"],
+                    choices=["xbatched", "mixed", "grad", "precision", "kgemm", "big", "rect",
+                             "small"],
                     default="xbatched")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -1069,6 +1121,8 @@ def main():
         return run_big(args)
     if args.workload == "rect":
         return run_rect(args)
+    if args.workload == "small":
+        return run_small(args)
     return run_ours(args)
 
 

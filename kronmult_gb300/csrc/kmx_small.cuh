@@ -7,12 +7,18 @@
 //   1. the chunk's X blocks and factors are staged in shared memory -- for
 //      the contiguous batched layout with 128-bit loads over the whole chunk
 //      (every byte of a sector used), otherwise entry by entry through the
-//      pointer arrays; the factors are stored row-major (row = output index);
+//      pointer arrays; the factors are stored column-major as applied, so
+//      the threads of a mode, which read different rows at the same column,
+//      read consecutive words (a row-major copy put every row on the same
+//      banks: 136 shared-memory bank conflicts per d=2 n=8 entry), and the
+//      batched layout's column-major factors copy straight across;
 //   2. the d modes are applied in the reference's order (A1 first), one
 //      thread per output element and mode, ping-ponging between two
 //      shared-memory buffers: the last mode adds its outputs to Y
 //      (read-modify-write where Y blocks are exclusive, atomics otherwise),
-//      consecutive threads on consecutive Y elements.
+//      consecutive threads on consecutive Y elements.  In the batched
+//      layout the chunk's Y blocks are staged with X (128-bit loads), so the
+//      last mode stores Y without waiting on a load.
 // Several CTAs per SM overlap one chunk's loads with another's arithmetic.
 //
 // Arithmetic policies: plain FMA in T; FP32 with each dot product rounded once
@@ -40,6 +46,8 @@ __host__ __device__ constexpr bool supported(int NN, int D) {
 }
 
 // Plain forms: V == In == Out == T.
+// dot(a, v, vs): sum_j a[j * NN] v[j * vs] (a: one row of a column-major
+// factor).
 template <typename T, bool RD>
 struct SmallPlain {
   using In = T;
@@ -47,7 +55,10 @@ struct SmallPlain {
   static constexpr bool SPLIT = false;
   template <int NN>
   __device__ __forceinline__ static V dot(const V* a, const V* v, int vs) {
-    return dot_n<T, RD, NN>(a, v, vs);
+    V av[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) av[j] = a[j * NN];
+    return dot_n<T, RD, NN>(av, v, vs);
   }
 };
 
@@ -58,10 +69,13 @@ struct SmallSplit {
   static constexpr bool SPLIT = true;
   template <int NN>
   __device__ __forceinline__ static V dot(const V* a, const V* v, int vs) {
-    df vv[NN];
+    df av[NN], vv[NN];
 #pragma unroll
-    for (int j = 0; j < NN; ++j) vv[j] = v[j * vs];
-    return df_dot<NN>(a, vv);
+    for (int j = 0; j < NN; ++j) {
+      av[j] = a[j * NN];
+      vv[j] = v[j * vs];
+    }
+    return df_dot<NN>(av, vv);
   }
 };
 
@@ -77,8 +91,8 @@ struct Layout {
   // the double-float form keeps the squares of the last mode's outputs for
   // the guard's per-entry norm (one float per output)
   static constexpr int SQ = Pol::SPLIT ? N * 4 : 0;
-  static constexpr int PER_ENTRY =
-      (NA + NBUF * N) * (int)sizeof(V) + SQ + (D + 2) * 8 + 4 * (D + 1) + 4 * (D + 2) + 4;
+  static constexpr int PER_ENTRY = (NA + NBUF * N) * (int)sizeof(V) + N * (int)sizeof(V) + SQ +
+                                   (D + 2) * 8 + 4 * (D + 1) + 4 * (D + 2) + 4;
   static constexpr int K0 = CHUNK_BYTES / PER_ENTRY;
   static constexpr int K = K0 < 1 ? 1 : (K0 > 512 ? 512 : K0);
   // byte offsets, every region 16-byte aligned (the staging stores are 128-bit)
@@ -86,7 +100,8 @@ struct Layout {
   static constexpr int A_OFF = 0;
   static constexpr int W0_OFF = al16(A_OFF + K * NA * (int)sizeof(V));
   static constexpr int W1_OFF = al16(W0_OFF + K * N * (int)sizeof(V));
-  static constexpr int SQ_OFF = al16(W1_OFF + (NBUF == 2 ? K * N * (int)sizeof(V) : 0));
+  static constexpr int YS_OFF = al16(W1_OFF + (NBUF == 2 ? K * N * (int)sizeof(V) : 0));  // staged Y
+  static constexpr int SQ_OFF = al16(YS_OFF + K * N * (int)sizeof(V));
   static constexpr int PX_OFF = al16(SQ_OFF + K * SQ);
   static constexpr int PY_OFF = PX_OFF + K * 8;
   static constexpr int PA_OFF = PY_OFF + K * 8;
@@ -96,10 +111,10 @@ struct Layout {
   static constexpr int BYTES = al16(FLAG_OFF + K * 4 + 16);        // + redo count
 };
 
-// Row i_k of factor k of chunk entry e, row-major.
+// Row i_k of factor k of chunk entry e (column-major: its entries NN apart).
 template <int NN, int D, typename V>
 __device__ __forceinline__ const V* factor_row(const V* sA, int e, int k, int i) {
-  return sA + ((e * D + k) * NN + i) * NN;
+  return sA + (e * D + k) * NN * NN + i;
 }
 
 // The FP64 recursion of one chunk entry, by the whole CTA, on its slices of
@@ -157,10 +172,12 @@ __global__ void __launch_bounds__(THREADS) small_kernel(const Problem p) {
   float* sNrm = reinterpret_cast<float*>(smem + L::NRM_OFF);
   int* sFlag = reinterpret_cast<int*>(smem + L::FLAG_OFF);
   float* sSq = reinterpret_cast<float*>(smem + L::SQ_OFF);  // [K][N] (split)
+  In* sYs = reinterpret_cast<In*>(smem + L::YS_OFF);        // [K][N] staged Y (batched)
   const bool excl = p.y_exclusive != 0;
   const long long total = launch_count(p);
   const long long nchunks = (total + K - 1) / K;
   const bool contig = p.layout == L_BATCHED && !p.order;
+  const bool ystaged = contig && excl;
   // per-entry reductions of the double-float form: ES threads per entry (a
   // warp when the entry has 64 or more values, else one thread)
   constexpr int ES = (N + NA >= 64) ? 32 : 1;
@@ -197,23 +214,32 @@ __global__ void __launch_bounds__(THREADS) small_kernel(const Problem p) {
       const long long ent0 = pos0 + p.entry_offset;
       const In* xg = static_cast<const In*>(p.X) + ent0 * N;
       const int nx = kc * N;
-      if ((reinterpret_cast<uintptr_t>(xg) & 15) == 0) {
-        constexpr int PV = 16 / (int)sizeof(In);  // values per 128-bit load
-        const int nv = nx / PV;
-        for (int i = threadIdx.x; i < nv; i += THREADS) {
-          const uint4 u = __ldg(reinterpret_cast<const uint4*>(xg) + i);
-          *reinterpret_cast<uint4*>(rawX + i * PV) = u;
+      // X, and Y where the blocks are exclusive, into shared memory
+      auto stage = [&](const In* g, In* sm) {
+        if ((reinterpret_cast<uintptr_t>(g) & 15) == 0) {
+          constexpr int PV = 16 / (int)sizeof(In);  // values per 128-bit load
+          const int nv = nx / PV;
+          for (int i = threadIdx.x; i < nv; i += THREADS) {
+            const uint4 u = __ldg(reinterpret_cast<const uint4*>(g) + i);
+            *reinterpret_cast<uint4*>(sm + i * PV) = u;
+          }
+          for (int i = nv * PV + threadIdx.x; i < nx; i += THREADS) sm[i] = __ldg(g + i);
+        } else {
+          for (int i = threadIdx.x; i < nx; i += THREADS) sm[i] = __ldg(g + i);
         }
-        for (int i = nv * PV + threadIdx.x; i < nx; i += THREADS) rawX[i] = __ldg(xg + i);
-      } else {
-        for (int i = threadIdx.x; i < nx; i += THREADS) rawX[i] = __ldg(xg + i);
-      }
-      // factors: (n, n, d, batch) column-major, ld = n
+      };
+      stage(xg, rawX);
+      if (ystaged) stage(static_cast<const In*>(p.Y) + ent0 * N, sYs);
+      // factors: (n, n, d, batch) column-major, ld = n: the same layout
+      // (transposed factors swap row and column)
       const In* ag = static_cast<const In*>(p.A) + ent0 * NA;
       for (int i = threadIdx.x; i < kc * NA; i += THREADS) {
-        const int e = i / NA, m = i - e * NA, l = m / (NN * NN), rc = m - l * NN * NN;
-        const int row = rc % NN, col = rc / NN;  // stored A(row, col)
-        const int dst = p.trans ? ((e * D + l) * NN + col) * NN + row : ((e * D + l) * NN + row) * NN + col;
+        int dst = i;
+        if (p.trans) {
+          const int e = i / NA, m = i - e * NA, l = m / (NN * NN), rc = m - l * NN * NN;
+          const int row = rc % NN, col = rc / NN;  // stored A(row, col)
+          dst = (e * D + l) * NN * NN + row * NN + col;
+        }
         rawA[dst] = __ldg(ag + i);
       }
     } else {
@@ -224,7 +250,7 @@ __global__ void __launch_bounds__(THREADS) small_kernel(const Problem p) {
       }
       for (int i = threadIdx.x; i < kc * NA; i += THREADS) {
         const int e = i / NA, m = i - e * NA, l = m / (NN * NN), rc = m - l * NN * NN;
-        const int row = rc / NN, col = rc % NN;  // applied M(row, col)
+        const int row = rc % NN, col = rc / NN;  // applied M(row, col), column-major
         const In* ap = sPA[e * D + l];
         const long long ld = p.ld[l];
         rawA[i] = ap ? (p.trans ? ap[col + row * ld] : ap[row + col * ld]) : In(0);
@@ -289,8 +315,11 @@ __global__ void __launch_bounds__(THREADS) small_kernel(const Problem p) {
     }
     __syncthreads();
     // ---- the d modes, A1 first; the last adds to Y ----
+    // first pass (only < 0, neg false) with staged Y: plain stores of the
+    // staged value plus the contribution; other passes read-modify-write
     auto last_mode = [&](const V* src, bool neg, bool norm, int only) {
       constexpr int k = D - 1;
+      const bool st = ystaged && only < 0 && !neg;
       for (int i = threadIdx.x; i < kc * N; i += THREADS) {
         const int e = i / N, q = i - e * N;
         if (only >= 0 && e != only) continue;
@@ -304,10 +333,18 @@ __global__ void __launch_bounds__(THREADS) small_kernel(const Problem p) {
 #pragma unroll
           for (int l = 0; l <= D; ++l) escale += sExp[e * (D + 1) + l] - 1023;
           const double y = tile::SplitPolicy::finish(v, escale);
-          y_accumulate(sPY[e] + q, neg ? -y : y, excl);
+          if (st) {
+            sPY[e][q] = sYs[i] + y;
+          } else {
+            y_accumulate(sPY[e] + q, neg ? -y : y, excl);
+          }
         } else {
           if (fl & SF_NULL) continue;
-          y_accumulate(sPY[e] + q, v, excl);
+          if (st) {
+            sPY[e][q] = sYs[i] + v;
+          } else {
+            y_accumulate(sPY[e] + q, v, excl);
+          }
         }
       }
     };
