@@ -19,7 +19,7 @@ import torch
 from . import _lib, kronmult_batched
 
 
-def _grad_call(d, n, A, X, G, Y, dX, dA, W, form=None):
+def _grad_call(d, n, A, X, G, Y, dX, dA, W, form=None, engine=None):
     L = _lib.lib()
     f64 = A.dtype == torch.float64
 
@@ -29,7 +29,10 @@ def _grad_call(d, n, A, X, G, Y, dX, dA, W, form=None):
     cap = W.numel() * W.element_size() if W is not None else 0
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     if f64:
-        opt = None if form is None else C.byref(_lib.options(form))
+        opt = None
+        if form is not None or engine is not None:
+            opt = C.byref(_lib.options(form if form is not None else "auto",
+                                       engine=engine if engine is not None else "tuned"))
         rc = L.kmx_kronmult_batched_grad_f64_ex(d, n, a(A), a(X), a(G), a(Y), a(dX), a(dA), a(W),
                                                 cap, A.shape[0], opt, s)
     else:
@@ -49,15 +52,17 @@ def grad_workspace(d, n, batch, dtype=torch.float64, device="cuda"):
     return torch.empty((nbytes + esz - 1) // esz, dtype=dtype, device=device)
 
 
-def kronmult_fused_grad(A, X, G, want_y=True, form=None):
+def kronmult_fused_grad(A, X, G, want_y=True, form=None, engine=None):
     """Y, dX, dA of loss = sum(G * Y) in one launch.  form: None (the library
-    default: double-float for FP64), "split", or "plain" (native FP64)."""
+    default: double-float for FP64), "split", or "plain" (native FP64).
+    engine: None (one warp per entry where the entry fits, else a CTA per
+    entry) or "per_mode" (a CTA per entry)."""
     batch, d, n, _ = A.shape
     Y = torch.zeros_like(X) if want_y else None
     dX = torch.zeros_like(X)
     dA = torch.zeros_like(A)
     _grad_call(d, n, A.contiguous(), X.contiguous(), G.contiguous(), Y, dX, dA,
-               grad_workspace(d, n, batch, A.dtype), form)
+               grad_workspace(d, n, batch, A.dtype), form, engine)
     return Y, dX, dA
 
 

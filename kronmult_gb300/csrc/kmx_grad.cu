@@ -18,27 +18,10 @@
 
 #include "../../include/kronmult_gb300.h"
 #include "kmx_engine.cuh"
+#include "kmx_grad.h"
 #include "kmx_launch.cuh"
 
 namespace kmx {
-
-struct GradProblem {
-  int d;
-  int N;
-  int batch;
-  const void* A;   // (n, n, d, batch) column-major
-  const void* X;   // (N, batch)
-  const void* G;   // (N, batch)
-  void* Y;         // (N, batch) or null
-  void* dX;        // (N, batch) or null
-  void* dA;        // (n, n, d, batch) or null
-  void* W;         // global slots for the forward intermediates (or null)
-  long long wslot; // elements per slot
-  int nslots;
-  int f_in_smem;   // forward intermediates in shared memory
-  int exp_off;     // split kernel: byte offset of the per-entry exponents in shared memory
-  int* status;
-};
 
 namespace {
 
@@ -630,9 +613,12 @@ GradPlan grad_plan(int d, int n, long long N, int max_smem) {
 
 // form: KMX_FORM_PLAIN runs FP64 (FP32) arithmetic; any other form runs the
 // double-float kernel for FP64 data.
+// engine: KMX_ENGINE_PER_MODE runs the CTA-per-entry kernels above; any other
+// value runs FP64 data one warp per entry (kmx_grad_warp.cu) where the entry's
+// factors and intermediates fit in the warp's share of shared memory.
 template <typename T>
 int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* dA, T* W,
-              size_t Wbytes, int batch, int form, cudaStream_t s) {
+              size_t Wbytes, int batch, int form, int engine, cudaStream_t s) {
   if (d < 1 || d > MAXD || n < 1 || batch < 0) return KMX_ERR_INVALID_ARG;
   if (form != KMX_FORM_AUTO && form != KMX_FORM_PLAIN && form != KMX_FORM_SPLIT &&
       form != KMX_FORM_DIGITS)
@@ -660,6 +646,16 @@ int grad_impl(int d, int n, const T* A, const T* X, const T* G, T* Y, T* dX, T* 
   gp.dA = dA;
   gp.W = W;
   gp.wslot = (long long)(d > 1 ? d - 1 : 1) * N;
+  if (sizeof(T) == 8 && engine != KMX_ENGINE_PER_MODE && grad_warp_bytes(d, n) > 0) {
+    int rc = device_status_ptr(&gp.status);
+    if (rc != KMX_OK) return rc;
+    gp.W = nullptr;
+    gp.wslot = 0;
+    gp.nslots = 0;
+    gp.f_in_smem = 1;
+    gp.exp_off = 0;
+    return launch_grad_warp(gp, n, split, s);
+  }
   const GradPlan plan = grad_plan<T>(d, n, N, di.max_smem_optin);
   if (!plan.ok) return KMX_ERR_UNSUPPORTED;
   const int threads = plan.threads;
@@ -718,7 +714,8 @@ extern "C" int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, cons
                                              double* W, size_t Wcapacity_bytes, int batchCount,
                                              kmx_stream_t stream) {
   return kmx::grad_impl<double>(d, n, A, X, G, Y, dX, dA, W, Wcapacity_bytes, batchCount,
-                                default_form(), reinterpret_cast<cudaStream_t>(stream));
+                                default_form(), KMX_ENGINE_TUNED,
+                                reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int kmx_kronmult_batched_grad_f64_ex(int d, int n, const double* A, const double* X,
@@ -728,6 +725,7 @@ extern "C" int kmx_kronmult_batched_grad_f64_ex(int d, int n, const double* A, c
                                                 kmx_stream_t stream) {
   return kmx::grad_impl<double>(d, n, A, X, G, Y, dX, dA, W, Wcapacity_bytes, batchCount,
                                 opt ? opt->form : default_form(),
+                                opt ? opt->engine : KMX_ENGINE_TUNED,
                                 reinterpret_cast<cudaStream_t>(stream));
 }
 
@@ -736,5 +734,6 @@ extern "C" int kmx_kronmult_batched_grad_f32(int d, int n, const float* A, const
                                              float* W, size_t Wcapacity_bytes, int batchCount,
                                              kmx_stream_t stream) {
   return kmx::grad_impl<float>(d, n, A, X, G, Y, dX, dA, W, Wcapacity_bytes, batchCount,
-                               KMX_FORM_PLAIN, reinterpret_cast<cudaStream_t>(stream));
+                               KMX_FORM_PLAIN, KMX_ENGINE_TUNED,
+                               reinterpret_cast<cudaStream_t>(stream));
 }
