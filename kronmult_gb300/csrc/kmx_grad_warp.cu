@@ -29,6 +29,7 @@
 #include "kmx_engine.cuh"
 #include "kmx_grad.h"
 #include "kmx_launch.cuh"
+#include "kmx_pack.cuh"
 
 namespace kmx {
 namespace gw {
@@ -53,8 +54,9 @@ __host__ __device__ constexpr int slot_words(int n, int N) {
 // Per-warp region in 8-byte words: the factors (FP64 row-major, or for the
 // packed double-float form two row-pair copies, A_l and A_l^T), d+1 slots and
 // the Gram partials [32][n].
+__host__ __device__ constexpr bool packed_form(int n) { return (n & 1) == 0 && n <= 4; }
 __host__ __device__ constexpr int factor_words(int n, int d) {
-  return ((n & 1) == 0 ? 2 : 1) * d * n * n;
+  return (packed_form(n) ? 2 : 1) * d * n * n;
 }
 __host__ __device__ constexpr int warp_words(int d, int n) {
   return (factor_words(n, d) + (d + 1) * slot_words(n, ipow(n, d)) + 32 * n + 1) / 2 * 2;
@@ -69,6 +71,7 @@ __host__ __device__ constexpr bool warp_fits(int d, int n) {
 // Double-float pairs at per-entry power-of-two scales (kmx_engine.cuh).
 struct WDf {
   using V = df;
+  static constexpr bool PACKED = false;
   __device__ static __forceinline__ V make(double x, int e) { return split_scaled(x, e); }
   template <int NN>
   __device__ static __forceinline__ V dot(const V* a, const V* v) {
@@ -98,6 +101,7 @@ struct WDf {
 // Native FP64 (the scales are ignored).
 struct WF64 {
   using V = double;
+  static constexpr bool PACKED = false;
   __device__ static __forceinline__ V make(double x, int) { return x; }
   template <int NN>
   __device__ static __forceinline__ V dot(const V* a, const V* v) {
@@ -114,6 +118,43 @@ struct WF64 {
     __device__ __forceinline__ void add(V a, V b) { s = __fma_rn(a, b, s); }
     __device__ __forceinline__ V get() const { return s; }
   };
+};
+
+// Double-float on packed FP32 pairs (kmx_pack.cuh), n = 2, 4: the mode
+// products form the dot products of two output rows per instruction from
+// factor row pairs (A_l and A_l^T each stored as row pairs), and the Gram sums
+// accumulate two columns b, b+1 per instruction.  Values in the slots, the
+// widening and the partial sums are those of WDf.  (Measured on GB300: d=4
+// n=4 0.105 -> 0.091 ms, d=6 n=2 0.163 -> 0.155; n = 6, 8 gained nothing, d=3
+// n=6 lost 5 %, so they keep the scalar pairs and half the factor storage.)
+struct WPk : WDf {
+  static constexpr bool PACKED = true;
+};
+
+// Running double-float sums of two columns: the negated sum of the high
+// products (ns) and the FP32 sum of everything else (c), as in pk2::dot_pair.
+struct PkSum {
+  pk2::u64 ns, c;
+  __device__ __forceinline__ void zero() { ns = c = 0ull; }
+  // += (fh, fl) * b for the pair of values (fh, fl) and b = (bh, bl) broadcast
+  __device__ __forceinline__ void add(pk2::u64 fh, pk2::u64 fl, pk2::u64 bh, pk2::u64 bl,
+                                      pk2::u64 nbh) {
+    const pk2::u64 q = pk2::mul(fh, nbh);  // -p, rounded
+    pk2::u64 e = pk2::fma(fh, bh, q);      // f b - p, exact
+    e = pk2::fma(fh, bl, e);
+    e = pk2::fma(fl, bh, e);
+    pk2::u64 t, te;
+    pk2::two_sum(ns, q, t, te);  // -(s + p) exactly as t + te
+    ns = t;
+    c = pk2::add(c, pk2::sub(e, te));
+  }
+  // the two sums as normalised pairs
+  __device__ __forceinline__ void get(df& v0, df& v1) const {
+    const pk2::u64 hi = pk2::sub(c, ns);
+    const pk2::u64 lo = pk2::sub(c, pk2::add(hi, ns));
+    pk2::unpack(hi, v0.hi, v1.hi);
+    pk2::unpack(lo, v0.lo, v1.lo);
+  }
 };
 
 // ---- steps of one entry (every lane of the warp calls them) -----------------
@@ -155,6 +196,37 @@ __device__ __forceinline__ void mode_step(const typename P::V* src, typename P::
   }
 }
 
+// Packed form of mode_step: one fiber at a time, each input value broadcast
+// to both halves (and negated: kmx_pack.cuh), the dot products of output rows
+// (2rp, 2rp+1) from the row pairs F[rp*NN + j] of A_K (or of A_K^T).
+template <int NN, int D, int K>
+__device__ __forceinline__ void mode_step_pk(const df* src, df* dst, const pk2::RowPair* F,
+                                             int lane) {
+  using pk2::u64;
+  constexpr int S = ipow(NN, D - 1 - K), NF = ipow(NN, D - 1), RP = NN / 2;
+  for (int f = lane; f < NF; f += 32) {
+    const int base = (f / S) * NN * S + f % S;
+    u64 vh[NN], vl[NN], nvh[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) {
+      const df v = src[ps<NN>(base + j * S)];
+      vh[j] = pk2::bcast(v.hi);
+      vl[j] = pk2::bcast(v.lo);
+      nvh[j] = pk2::bcast(-v.hi);
+    }
+#pragma unroll(NN <= 4 ? RP : 2)
+    for (int rp = 0; rp < RP; ++rp) {
+      u64 oh, ol;
+      pk2::dot_pair<NN>(F + rp * NN, vh, vl, nvh, oh, ol);
+      df o0, o1;
+      pk2::unpack(oh, o0.hi, o1.hi);
+      pk2::unpack(ol, o0.lo, o1.lo);
+      dst[ps<NN>(base + 2 * rp * S)] = o0;
+      dst[ps<NN>(base + (2 * rp + 1) * S)] = o1;
+    }
+  }
+}
+
 // out[q] += 2^esc src[q], q < N: coalesced, four loads in flight per lane.
 template <class P, int NN, int N>
 __device__ __forceinline__ void add_out(double* out, const typename P::V* src, int esc, int lane) {
@@ -183,18 +255,37 @@ __device__ __forceinline__ void gram_step(const typename P::V* B, const typename
   constexpr int SG = 32 / NN;
   const int a = lane / SG, sub = lane - a * SG;
   if (a < NN) {
-    typename P::Acc acc[NN];
+    if constexpr (P::PACKED) {
+      PkSum acc[NN / 2];
 #pragma unroll
-    for (int b = 0; b < NN; ++b) acc[b].zero();
+      for (int b = 0; b < NN / 2; ++b) acc[b].zero();
 #pragma unroll 2
-    for (int f = sub; f < NF; f += SG) {
-      const int base = (f / S) * NN * S + f % S;
-      const V bv = B[ps<NN>(base + a * S)];
+      for (int f = sub; f < NF; f += SG) {
+        const int base = (f / S) * NN * S + f % S;
+        const df bv = B[ps<NN>(base + a * S)];
+        const pk2::u64 bh = pk2::bcast(bv.hi), bl = pk2::bcast(bv.lo), nbh = pk2::bcast(-bv.hi);
 #pragma unroll
-      for (int b = 0; b < NN; ++b) acc[b].add(bv, Fk[ps<NN>(base + b * S)]);
+        for (int b = 0; b < NN / 2; ++b) {
+          const df f0 = Fk[ps<NN>(base + 2 * b * S)], f1 = Fk[ps<NN>(base + (2 * b + 1) * S)];
+          acc[b].add(pk2::pack(f0.hi, f1.hi), pk2::pack(f0.lo, f1.lo), bh, bl, nbh);
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < NN / 2; ++b) acc[b].get(part[lane * NN + 2 * b], part[lane * NN + 2 * b + 1]);
+    } else {
+      typename P::Acc acc[NN];
+#pragma unroll
+      for (int b = 0; b < NN; ++b) acc[b].zero();
+#pragma unroll 2
+      for (int f = sub; f < NF; f += SG) {
+        const int base = (f / S) * NN * S + f % S;
+        const V bv = B[ps<NN>(base + a * S)];
+#pragma unroll
+        for (int b = 0; b < NN; ++b) acc[b].add(bv, Fk[ps<NN>(base + b * S)]);
+      }
+#pragma unroll
+      for (int b = 0; b < NN; ++b) part[lane * NN + b] = acc[b].get();
     }
-#pragma unroll
-    for (int b = 0; b < NN; ++b) part[lane * NN + b] = acc[b].get();
   }
   __syncwarp();
   for (int t = lane; t < NN * NN; t += 32) {
@@ -225,11 +316,24 @@ struct Region {
   }
 };
 
+// Mode K with A_K (TR: A_K^T) from src into dst, in the policy's arithmetic.
+// Factor storage: FP64 / WDf row-major sA[K*NN2 + a*NN + j]; WPk row pairs,
+// A_K at (2K)*NN2/2 and A_K^T at (2K+1)*NN2/2 RowPairs.
+template <class P, int NN, int D, int K, bool TR>
+__device__ __forceinline__ void apply_mode(const Region<P, NN, D>& r, const typename P::V* src,
+                                           typename P::V* dst, int lane) {
+  if constexpr (P::PACKED) {
+    const pk2::RowPair* F = reinterpret_cast<const pk2::RowPair*>(r.sA) + (2 * K + (TR ? 1 : 0)) * (NN * NN / 2);
+    mode_step_pk<NN, D, K>(src, dst, F, lane);
+  } else {
+    mode_step<P, NN, D, K, TR>(src, dst, r.sA + K * NN * NN, lane);
+  }
+}
+
 template <class P, int NN, int D, int K>
 __device__ __forceinline__ void fwd_sweep(const Region<P, NN, D>& r, int lane) {
   if constexpr (K + 1 < D) {
-    mode_step<P, NN, D, K, false>(r.slots + K * r.SL, r.slots + (K + 1) * r.SL,
-                                  r.sA + K * NN * NN, lane);
+    apply_mode<P, NN, D, K, false>(r, r.slots + K * r.SL, r.slots + (K + 1) * r.SL, lane);
     __syncwarp();
     fwd_sweep<P, NN, D, K + 1>(r, lane);
   }
@@ -242,11 +346,11 @@ __device__ __forceinline__ void bwd_sweep(const Region<P, NN, D>& r, double* dAe
     gram_step<P, NN, D, K>(r.Bs, r.slots + K * r.SL, r.part, dAe + K * NN * NN, esc_dA - sa[K],
                            lane);
   if constexpr (K > 0) {
-    mode_step<P, NN, D, K, true>(r.Bs, r.Bs, r.sA + K * NN * NN, lane);
+    apply_mode<P, NN, D, K, true>(r, r.Bs, r.Bs, lane);
     __syncwarp();
     bwd_sweep<P, NN, D, K - 1>(r, dAe, dXe, sa, esc_dA, esc_dX, lane);
   } else if (dXe) {  // slot 0 is free once the last Gram has read X
-    mode_step<P, NN, D, 0, true>(r.Bs, r.slots, r.sA, lane);
+    apply_mode<P, NN, D, 0, true>(r, r.Bs, r.slots, lane);
     __syncwarp();
     add_out<P, NN, ipow(NN, D)>(dXe, r.slots, esc_dX, lane);
   }
@@ -268,17 +372,53 @@ __device__ __forceinline__ void warp_entry(const GradProblem& gp, long long e, d
     sa_sum += sa[l];
   }
   const int sx = ex - 1023, sg = eg - 1023;
-  if constexpr (!std::is_same<V, double>::value) {
-    // FP64 -> scaled pairs in place (each lane converts what it staged)
+  if constexpr (P::PACKED) {
+    // FP64 row-major -> row pairs of A_l and of A_l^T (twice the space, so
+    // every lane reads its values before any lane writes)
+    constexpr int RP = NN / 2, NRP = D * NN2, PER = (NRP + 31) / 32;
+    const double* raw = reinterpret_cast<const double*>(r.sA);
+    double x0[PER], x1[PER];
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+      const int idx = lane + 32 * t;
+      x0[t] = x1[t] = 0.0;
+      if (idx < NRP) {
+        const int j = idx % NN, rp = (idx / NN) % RP, lo = idx / (NN * RP);  // lo = 2l + TR
+        const double* Al = raw + (lo >> 1) * NN2;
+        if (lo & 1) {  // A^T(2rp, j) = A(j, 2rp)
+          x0[t] = Al[j * NN + 2 * rp];
+          x1[t] = Al[j * NN + 2 * rp + 1];
+        } else {
+          x0[t] = Al[(2 * rp) * NN + j];
+          x1[t] = Al[(2 * rp + 1) * NN + j];
+        }
+      }
+    }
+    __syncwarp();
+    pk2::RowPair* pk = reinterpret_cast<pk2::RowPair*>(r.sA);
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+      const int idx = lane + 32 * t;
+      if (idx < NRP) {
+        const int e = ea[idx / (NN * RP * 2)];
+        const df s0 = split_scaled(x0[t], e), s1 = split_scaled(x1[t], e);
+        pk[idx].hi = pk2::pack(s0.hi, s1.hi);
+        pk[idx].lo = pk2::pack(s0.lo, s1.lo);
+      }
+    }
+  } else if constexpr (!std::is_same<V, double>::value) {
     for (int i = lane; i < D * NN2; i += 32)
       r.sA[i] = P::make(reinterpret_cast<const double*>(r.sA)[i], ea[i / NN2]);
+  }
+  if constexpr (!std::is_same<V, double>::value) {
+    // X: FP64 -> scaled pairs in place (each lane converts what it staged)
     for (int q = lane; q < N; q += 32)
       r.slots[ps<NN>(q)] = P::make(reinterpret_cast<const double*>(r.slots)[ps<NN>(q)], ex);
     __syncwarp();
   }
   fwd_sweep<P, NN, D, 0>(r, lane);
   if (gp.Y) {  // the last mode into slot D, then Y += it
-    mode_step<P, NN, D, D - 1, false>(r.slots + (D - 1) * r.SL, r.Bs, r.sA + (D - 1) * NN2, lane);
+    apply_mode<P, NN, D, D - 1, false>(r, r.slots + (D - 1) * r.SL, r.Bs, lane);
     __syncwarp();
     add_out<P, NN, N>(static_cast<double*>(gp.Y) + e * N, r.Bs, sx + sa_sum, lane);
     __syncwarp();
@@ -382,7 +522,8 @@ __global__ void __launch_bounds__(256, 2) grad_warp_kernel(const GradProblem gp)
       if (special) {
         warp_entry_f64<NN, D>(gp, e, wbase, lane);
       } else {
-        warp_entry<WDf, NN, D>(gp, e, wbase, ea, ex, eg, lane);
+        using Pol = typename std::conditional<packed_form(NN), WPk, WDf>::type;
+        warp_entry<Pol, NN, D>(gp, e, wbase, ea, ex, eg, lane);
       }
     }
   }

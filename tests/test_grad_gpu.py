@@ -204,3 +204,42 @@ def test_split_grad_special_entries_run_fp64(kmx):
             assert np.array_equal(s_[b], p_[b]) or blockwise_rel_err(s_[b:b + 1], p_[b:b + 1]) <= 1e-13
     assert np.array_equal(dAs[3].cpu().numpy(), dAp[3].cpu().numpy())  # FP64 path taken
     assert np.abs(dAs[3, 2].cpu().numpy()).max() > 0
+
+
+# Shapes the warp-per-entry fused kernel takes (d >= 3 with the entry's
+# factors and intermediates in 32 KB of shared memory).
+WARP_SHAPES = [(3, 2), (3, 3), (3, 4), (3, 5), (3, 6), (3, 7), (3, 8), (4, 2), (4, 3), (4, 4),
+               (4, 5), (5, 2), (5, 3), (6, 2)]
+
+
+@pytest.mark.parametrize("form", GRAD_FORMS)
+@pytest.mark.parametrize("d,n", WARP_SHAPES)
+def test_warp_kernel_vs_explicit_and_cta_kernel(kmx, d, n, form):
+    """The warp-per-entry kernel (the default for these shapes) against the
+    explicit-Kronecker gradient, and against the CTA-per-entry kernel (engine
+    "per_mode") on a batch that leaves the last CTA's warps partly idle, with
+    nonzero outputs to accumulate into."""
+    from kronmult_gb300.autograd import _grad_call
+
+    rng = np.random.default_rng(1000 + 10 * d + n)
+    batch, N = 37, n ** d
+    A = rng.standard_normal((batch, d, n, n)) / np.sqrt(n)
+    X = rng.standard_normal((batch, N))
+    G = rng.standard_normal((batch, N))
+    Y0 = rng.standard_normal((batch, N))
+    dX0 = rng.standard_normal((batch, N))
+    dA0 = rng.standard_normal((batch, d, n, n))
+    At, Xt, Gt = (torch.from_numpy(t).cuda() for t in (A, X, G))
+    out = {}
+    for eng in ("tuned", "per_mode"):
+        Y, dX, dA = (torch.from_numpy(t.copy()).cuda() for t in (Y0, dX0, dA0))
+        _grad_call(d, n, At, Xt, Gt, Y, dX, dA, None, form, eng)
+        torch.cuda.synchronize()
+        out[eng] = [t.cpu().numpy() for t in (Y, dX, dA)]
+    assert kmx.check_device_status() == 0
+    ex_dX, ex_dA = explicit_grads(A[:5], X[:5], G[:5])
+    w = out["tuned"]
+    assert blockwise_rel_err(w[1][:5] - dX0[:5], ex_dX) <= 1e-13
+    assert blockwise_rel_err((w[2][:5] - dA0[:5]).reshape(5, -1), ex_dA.reshape(5, -1)) <= 1e-13
+    for a, b in zip(out["tuned"], out["per_mode"]):
+        assert blockwise_rel_err(a.reshape(batch, -1), b.reshape(batch, -1)) <= 1e-13
