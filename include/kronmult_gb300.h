@@ -330,7 +330,12 @@ size_t kmx_grad_workspace_bytes(int d, int n, int batchCount, int fp64);
 /* FP64 arithmetic form: the library default (kmx_set_default_options), whose
  * AUTO runs the mode products and Gram sums in double-float on the FP32 pipe
  * (entries holding Inf/NaN or an all-zero X, G or factor in FP64); _ex takes
- * it from opt->form (KMX_FORM_PLAIN: native FP64).  FP32 data: FP32 FMA. */
+ * it from opt->form (KMX_FORM_PLAIN: native FP64).  FP32 data: FP32 FMA.
+ * Kernels for FP64 data: one warp per entry, every intermediate in shared
+ * memory, for d >= 3 entries whose factors and d+1 intermediates fit in 32 KB
+ * (d=3 n<=8, d=4 n<=5, d=5 n<=3, d=6 n=2); otherwise one CTA per entry.
+ * _ex with opt->engine = KMX_ENGINE_PER_MODE takes the CTA-per-entry kernel
+ * for every shape. */
 int kmx_kronmult_batched_grad_f64(int d, int n, const double* A, const double* X,
                                   const double* G, double* Y, double* dX, double* dA,
                                   double* W, size_t Wcapacity_bytes, int batchCount,
