@@ -289,6 +289,380 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_stream_kernel(KgArgs<T> a) {
   }
 }
 
+// Bulk-copy streaming kernel for FP32 kgemm_nn with mm, kk <= 16 (the
+// kronmult short-wide contractions), warp-specialised: items are (entry,
+// chunk of 256 columns), grid-stride per CTA, cycling through KB_STAGES
+// shared-memory stages.
+//   producer warp: for each item, waits until its stage is empty, reads the
+//     entry's pointers and leading dimensions, writes A as row pairs
+//     (A(2rp, k), A(2rp+1, k)) and an item descriptor into the stage, and
+//     fetches the B chunk (kk x 256, contiguous when ldB == kk) and, for beta
+//     outside {0, 1}, the C chunk by cp.async.bulk, completing on the stage's
+//     "full" mbarrier -- up to KB_STAGES items ahead of the consumers;
+//   8 consumer warps: each thread forms one column of C from its B column and
+//     A, two rows per instruction on packed FP32 pairs with the same
+//     double-length accumulation (exact products, two-sums, one rounding) as
+//     Acc<float>; the results leave by one cp.async.bulk store (beta == 0, or
+//     the blend) or one cp.reduce.async.bulk .add (beta == 1: element-wise
+//     atomic adds, the reference's atomicAdd epilogue), after which the
+//     stage's "empty" mbarrier releases it to the producer.
+// Bulk copies cover each chunk from its first 16-byte boundary in whole 16-byte
+// units; the few elements before and after are read and written directly.
+// Items whose B or C is not contiguous (ldB != kk, ldC != mm) read and write
+// global memory directly, with the same arithmetic.  The pointer and A reads
+// of the producer run two and one items ahead.  The square shapes n = 2..8
+// are compiled with mm = kk = n as constants: with run-time sizes the
+// guarded, fully unrolled loops cost 3.7x the instructions (ncu, n = 4).
+// Waits are bounded: one that runs out flags DF_WAIT_TIMEOUT, waits once more
+// for the stage's copies and leaves.
+constexpr int KB_STAGES = 4;
+constexpr int KB_CONSUMERS = 256;
+constexpr int KB_THREADS = KB_CONSUMERS + 32;
+
+struct KbDesc {
+  float* C;
+  const float* B;
+  long long ldb, ldc;
+  int c0, cw, flag;  // flag: 0 direct, 1 bulk, 2 skip (bad pointer or shape)
+  // bulk items: the chunk's B (kk*cw floats) and C (mm*cw floats) are read
+  // and written by bulk copies from the first 16-byte boundary (head hb, hc
+  // floats) for mb, mc floats (multiples of 4); the head and the tail go
+  // directly to global memory
+  int hb, mb, hc, mc;
+  int pad;
+};
+
+__device__ __forceinline__ void kb_mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tile::smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void kb_store(float* dst, const float* src, uint32_t bytes, bool add) {
+  if (add) {
+    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;" ::"l"(
+                     dst),
+                 "r"(tile::smem_u32(src)), "r"(bytes)
+                 : "memory");
+  } else {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+                 "r"(tile::smem_u32(src)), "r"(bytes)
+                 : "memory");
+  }
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void kb_consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(KB_CONSUMERS) : "memory");
+}
+
+// One stage, in floats: B chunk, C chunk (each rounded to 16 bytes), the A
+// row pairs [8][16] (u64).  After the stages: full and empty mbarriers, the
+// item descriptors and a timeout flag.
+// (each chunk area has 4 floats in front for the head's shift)
+__host__ __device__ constexpr int kb_c_off(int kk) { return 4 + (kk * KB_CONSUMERS + 3) / 4 * 4; }
+__host__ __device__ constexpr int kb_a_off(int mm, int kk) {
+  return kb_c_off(kk) + 4 + (mm * KB_CONSUMERS + 3) / 4 * 4;
+}
+__host__ __device__ constexpr int kb_stage_floats(int mm, int kk) {
+  return kb_a_off(mm, kk) + 8 * KG_SMALL_DIM * 2;
+}
+__host__ __device__ constexpr size_t kb_smem_bytes(int mm, int kk) {
+  return (size_t)KB_STAGES * kb_stage_floats(mm, kk) * 4 + 2 * KB_STAGES * 8 +
+         KB_STAGES * sizeof(KbDesc) + 16;
+}
+
+// MM, KK: the shape as compile-time constants (the square kronmult shapes,
+// fully unrolled), or 0 for run-time mm, kk <= 16.
+template <int MM, int KK>
+__global__ void __launch_bounds__(KB_THREADS) kgemm_bulk_kernel(KgArgs<float> a) {
+  using pk2::u64;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int mm = MM ? MM : a.mm, kk = KK ? KK : a.kk, nn = a.nn;
+  constexpr int QN = KK ? KK : KG_SMALL_DIM;            // k loop bound
+  constexpr int RPN = MM ? (MM + 1) / 2 : KG_SMALL_DIM / 2;  // row-pair loop bound
+  const int SF = kb_stage_floats(mm, kk), COFF = kb_c_off(kk), AOFF = kb_a_off(mm, kk);
+  float* stg = reinterpret_cast<float*>(smem);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)KB_STAGES * SF * 4);
+  uint64_t* empty = full + KB_STAGES;
+  KbDesc* desc = reinterpret_cast<KbDesc*>(empty + KB_STAGES);
+  int* sstop = reinterpret_cast<int*>(desc + KB_STAGES);
+  const int chunks = (nn + KB_CONSUMERS - 1) / KB_CONSUMERS;
+  const bool beta0 = a.beta == 0.f, beta1 = a.beta == 1.f;
+  const int RP = (mm + 1) / 2;
+  if (tid == 0) {
+    for (int s = 0; s < KB_STAGES; ++s) {
+      tile::mbar_init(&full[s], 1);
+      tile::mbar_init(&empty[s], 1);
+    }
+    sstop[0] = 0;
+    tile::fence_mbar_init();
+  }
+  __syncthreads();
+
+  if (tid < 32) {  // ---- producer warp ----
+    // Software pipeline: an item's pointers are read two items ahead and its
+    // A values one item ahead, so their global latencies overlap the waits
+    // for free stages instead of adding up item after item.
+    const int lane = tid;
+    struct Ptrs {
+      const float* A;
+      const float* B;
+      float* C;
+      long long lda, ldb, ldc;
+      int e, c0;
+      bool ok;  // pointers present and leading dimensions valid
+    };
+    auto load_ptrs = [&](long long it, Ptrs& p) {
+      p.ok = false;
+      p.e = 0;
+      p.c0 = 0;
+      p.A = p.B = nullptr;
+      p.C = nullptr;
+      p.lda = p.ldb = p.ldc = 0;
+      if (it >= a.items) return;
+      p.e = (int)(it / chunks);
+      p.c0 = (int)(it - (long long)p.e * chunks) * KB_CONSUMERS;
+      p.A = a.A[p.e];
+      p.B = a.B[p.e];
+      p.C = a.C[p.e];
+      p.lda = a.ldA[p.e];
+      p.ldb = a.ldB[p.e];
+      p.ldc = a.ldC[p.e];
+    };
+    auto check = [&](Ptrs& p) {
+      const bool bad_ptr = p.C == nullptr || (kk > 0 && (p.A == nullptr || p.B == nullptr));
+      const bool bad_ld = !bad_ptr && (p.ldc < mm || (kk > 0 && (p.lda < mm || p.ldb < kk)));
+      p.ok = !bad_ptr && !bad_ld;
+      return bad_ptr ? DF_NULL_PTR : (bad_ld ? DF_BAD_SHAPE : 0);
+    };
+    constexpr int AV = 8 * KG_SMALL_DIM / 32;  // A row-pair slots per lane
+    auto load_a = [&](const Ptrs& p, float (&v0)[AV], float (&v1)[AV]) {
+#pragma unroll
+      for (int j = 0; j < AV; ++j) {
+        const int idx = lane + 32 * j;
+        v0[j] = v1[j] = 0.f;
+        if (p.ok && idx < RP * kk) {
+          const int rp = idx / kk, q = idx - rp * kk;
+          v0[j] = p.A[2 * rp + q * p.lda];
+          if (2 * rp + 1 < mm) v1[j] = p.A[2 * rp + 1 + q * p.lda];
+        }
+      }
+    };
+    Ptrs cur, nxt, nn2;
+    load_ptrs(blockIdx.x, cur);
+    load_ptrs(blockIdx.x + (long long)gridDim.x, nxt);
+    int bad_cur = check(cur);
+    float a0[AV], a1[AV];
+    load_a(cur, a0, a1);
+    for (int k = 0;; ++k) {
+      const long long it = blockIdx.x + (long long)k * gridDim.x;
+      if (it >= a.items) break;
+      const int s = k % KB_STAGES;
+      load_ptrs(it + 2LL * gridDim.x, nn2);  // two ahead
+      if (k >= KB_STAGES) {  // the consumers released the stage's previous item
+        bool ok = true;
+        if (lane == 0) ok = tile::mbar_wait(&empty[s], (uint32_t)(k / KB_STAGES - 1) & 1u);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) {
+          if (lane == 0) atomicOr(a.status, DF_WAIT_TIMEOUT);
+          return;  // the consumers' bounded waits end them
+        }
+      }
+      const int cw = min(KB_CONSUMERS, nn - cur.c0);
+      float* st = stg + (size_t)s * SF;
+      u64* sAp = reinterpret_cast<u64*>(st + AOFF);
+#pragma unroll
+      for (int j = 0; j < AV; ++j) {
+        const int idx = lane + 32 * j;
+        if (cur.ok && idx < RP * kk) {
+          const int rp = idx / kk, q = idx - rp * kk;
+          sAp[rp * KG_SMALL_DIM + q] = pk2::pack(a0[j], a1[j]);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        KbDesc dd;
+        dd.C = cur.C;
+        dd.B = cur.B;
+        dd.ldb = cur.ldb;
+        dd.ldc = cur.ldc;
+        dd.c0 = cur.c0;
+        dd.cw = cw;
+        dd.flag = 0;
+        dd.hb = dd.mb = dd.hc = dd.mc = 0;
+        dd.pad = 0;
+        if (!cur.ok) {
+          dd.flag = 2;
+          if (cur.c0 == 0) atomicOr(a.status, bad_cur);
+        } else if (kk > 0 && cur.ldb == kk && cur.ldc == mm) {
+          dd.flag = 1;
+          // aligned middle of each chunk: from the first 16-byte boundary,
+          // whole 16-byte units
+          const float* gB = cur.B + (long long)cur.c0 * kk;
+          const float* gC = cur.C + (long long)cur.c0 * mm;
+          const int nb = kk * cw, nc = mm * cw;
+          dd.hb = min(nb, (int)(((16 - (reinterpret_cast<uintptr_t>(gB) & 15)) & 15) >> 2));
+          dd.mb = (nb - dd.hb) / 4 * 4;
+          dd.hc = min(nc, (int)(((16 - (reinterpret_cast<uintptr_t>(gC) & 15)) & 15) >> 2));
+          dd.mc = (nc - dd.hc) / 4 * 4;
+        }
+        desc[s] = dd;
+        const bool loadc = !beta0 && !beta1;
+        const uint32_t tx = (dd.flag == 1) ? (uint32_t)(dd.mb + (loadc ? dd.mc : 0)) * 4u : 0u;
+        if (tx > 0) {
+          tile::fence_proxy_async();
+          tile::mbar_expect_tx(&full[s], tx);
+          if (dd.mb > 0)
+            tile::tma_load_1d(st + 4, cur.B + (long long)cur.c0 * kk + dd.hb, (uint32_t)dd.mb * 4u,
+                              &full[s]);
+          if (loadc && dd.mc > 0)
+            tile::tma_load_1d(st + COFF + 4, cur.C + (long long)cur.c0 * mm + dd.hc,
+                              (uint32_t)dd.mc * 4u, &full[s]);
+        } else {
+          kb_mbar_arrive(&full[s]);
+        }
+      }
+      __syncwarp();
+      // advance: the next item's A now (its pointers arrived last iteration)
+      cur = nxt;
+      nxt = nn2;
+      bad_cur = check(cur);
+      load_a(cur, a0, a1);
+    }
+    return;
+  }
+
+  // ---- consumer warps ----
+  const int ct = tid - 32;
+  const u64 alpha2 = pk2::bcast(a.alpha), beta2 = pk2::bcast(a.beta);
+  int last_stage = -1;
+  for (int k = 0;; ++k) {
+    const long long it = blockIdx.x + (long long)k * gridDim.x;
+    if (it >= a.items) break;
+    const int s = k % KB_STAGES;
+    const uint32_t par = (uint32_t)(k / KB_STAGES) & 1u;
+    if (ct == 0 && !tile::mbar_wait(&full[s], par)) {
+      atomicOr(a.status, DF_WAIT_TIMEOUT);
+      tile::mbar_wait(&full[s], par);  // the stage's copies, once more
+      sstop[0] = 1;
+    }
+    kb_consumer_sync();  // stage s has arrived (the leader saw its mbarrier)
+    if (sstop[0]) {
+      if (ct == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      return;
+    }
+    const KbDesc dd = desc[s];
+    float* st = stg + (size_t)s * SF;
+    const u64* sAp = reinterpret_cast<const u64*>(st + AOFF);
+    const bool bulk = dd.flag == 1;
+    if (dd.flag != 2 && ct < dd.cw) {
+      const int c = dd.c0 + ct;
+      // element e of this column's B / C: bulk items index the chunk (B at
+      // bb[e0b + q], staged in sB for hb <= e < hb + mb), direct items the
+      // column in global memory
+      const float* bb = bulk ? dd.B + (long long)dd.c0 * kk : dd.B + (long long)c * dd.ldb;
+      float* cb = bulk ? dd.C + (long long)dd.c0 * mm : dd.C + (long long)c * dd.ldc;
+      const int e0b = bulk ? ct * kk : 0, e0c = bulk ? ct * mm : 0;
+      const int hb = dd.hb, mb = dd.mb, hc = dd.hc, mc = dd.mc;
+      const float* sB = st + 4 - hb;
+      float* sC = st + COFF + 4 - hc;
+      u64 b2[QN], nb2[QN];
+      if (KK % 4 == 0 && KK > 0 && bulk && hb == 0 && e0b + QN <= mb) {  // 16-byte loads
+#pragma unroll
+        for (int q = 0; q < QN; q += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(sB + e0b + q);
+          const float w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            b2[q + u] = pk2::bcast(w[u]);
+            nb2[q + u] = pk2::bcast(-w[u]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < QN; ++q) {
+          if (KK || q < kk) {
+            const int e = e0b + q;
+            const float v = (e >= hb && e < hb + mb) ? sB[e] : __ldg(bb + e);
+            b2[q] = pk2::bcast(v);
+            nb2[q] = pk2::bcast(-v);
+          }
+        }
+      }
+#pragma unroll(MM ? RPN : 1)
+      for (int rp = 0; rp < (MM ? RPN : RP); ++rp) {
+        u64 ns = 0ull, cc = 0ull;
+#pragma unroll
+        for (int q = 0; q < QN; ++q) {
+          if (KK || q < kk) {
+            const u64 a2 = sAp[rp * KG_SMALL_DIM + q];
+            const u64 qq = pk2::mul(a2, nb2[q]);     // -p, rounded
+            const u64 ee = pk2::fma(a2, b2[q], qq);  // a b - p, exact
+            u64 t, te;
+            pk2::two_sum(ns, qq, t, te);
+            ns = t;
+            cc = pk2::add(cc, pk2::sub(ee, te));
+          }
+        }
+        // alpha (t + l) with one rounding, t + l = s + c renormalised
+        const u64 th = pk2::sub(cc, ns);
+        const u64 tl = pk2::sub(cc, pk2::add(th, ns));
+        u64 v = pk2::fma(alpha2, th, pk2::mul(alpha2, tl));
+        const int r0 = 2 * rp;
+        const bool two = r0 + 1 < mm;
+        // rows r0, r0 + 1 of column c: elements e, e + 1 (staged or global)
+        const int e = e0c + r0;
+        const bool in0 = e >= hc && e < hc + mc, in1 = e + 1 >= hc && e + 1 < hc + mc;
+        if (!beta0 && !beta1) {  // nn rounds alpha*c, then blends (kgemm_nn.hpp:390-399)
+          const float o0 = in0 ? sC[e] : cb[e];
+          const float o1 = two ? (in1 ? sC[e + 1] : cb[e + 1]) : 0.f;
+          v = pk2::fma(beta2, pk2::pack(o0, o1), v);
+        }
+        if (MM % 2 == 0 && MM > 0 && hc == 0 && in0 && in1) {  // one 8-byte store
+          *reinterpret_cast<u64*>(sC + e) = v;
+        } else {
+          float v0, v1;
+          pk2::unpack(v, v0, v1);
+          if (in0) {
+            sC[e] = v0;
+          } else if (beta1) {
+            atomicAdd(cb + e, v0);
+          } else {
+            cb[e] = v0;
+          }
+          if (two) {
+            if (in1) {
+              sC[e + 1] = v1;
+            } else if (beta1) {
+              atomicAdd(cb + e + 1, v1);
+            } else {
+              cb[e + 1] = v1;
+            }
+          }
+        }
+      }
+    }
+    if (bulk) tile::fence_proxy_async();  // results visible to the bulk copy
+    kb_consumer_sync();                   // every column done; B and C read
+    if (ct == 0) {
+      // issue this item's result copy, then release the PREVIOUS item's stage
+      // once every copy but this one has read its source (waiting for this
+      // one's read here would put it on every item's path)
+      if (bulk && dd.mc > 0)
+        kb_store(dd.C + (long long)dd.c0 * mm + dd.hc, st + COFF + 4, (uint32_t)dd.mc * 4u, beta1);
+      else
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");  // an empty group keeps the count
+      if (k > 0) {
+        asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        kb_mbar_arrive(&empty[(k + KB_STAGES - 1) % KB_STAGES]);
+      }
+    }
+    last_stage = s;
+  }
+  if (ct == 0) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (last_stage >= 0) kb_mbar_arrive(&empty[last_stage]);
+  }
+}
+
 struct KgConfig {
   const void* func;
   int bm, bn;
@@ -317,8 +691,25 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   // the register tiles' several outputs per thread measure faster)
   const bool stream = sizeof(T) == 4 && !small && kk <= KG_SMALL_DIM &&
                       (trans_b ? (nn <= KG_SMALL_DIM) : (mm <= KG_SMALL_DIM));
+  // the nn streaming shapes take the bulk-copy kernel
+  const bool bulk = stream && !trans_b;
   KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
-  if (stream) {
+  size_t smem = 0;
+  if (bulk) {
+    switch (mm == kk ? mm : 0) {
+      case 2: cfg.func = (const void*)kgemm_bulk_kernel<2, 2>; break;
+      case 3: cfg.func = (const void*)kgemm_bulk_kernel<3, 3>; break;
+      case 4: cfg.func = (const void*)kgemm_bulk_kernel<4, 4>; break;
+      case 5: cfg.func = (const void*)kgemm_bulk_kernel<5, 5>; break;
+      case 6: cfg.func = (const void*)kgemm_bulk_kernel<6, 6>; break;
+      case 7: cfg.func = (const void*)kgemm_bulk_kernel<7, 7>; break;
+      case 8: cfg.func = (const void*)kgemm_bulk_kernel<8, 8>; break;
+      default: cfg.func = (const void*)kgemm_bulk_kernel<0, 0>; break;
+    }
+    cfg.bm = mm;
+    cfg.bn = KB_CONSUMERS;
+    smem = kb_smem_bytes(mm, kk);
+  } else if (stream) {
     cfg.func = trans_b ? (const void*)kgemm_stream_kernel<T, true>
                        : (const void*)kgemm_stream_kernel<T, false>;
     // items: (entry, chunk of KG_THREADS along the long dimension)
@@ -350,14 +741,17 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return KMX_ERR_CUDA;
   const DeviceInfo di = device_info(dev);
+  if (smem > 0 && ensure_smem(cfg.func, dev, smem) != cudaSuccess) return KMX_ERR_CUDA;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.func, KG_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.func, bulk ? KB_THREADS : KG_THREADS,
+                                                smem);
   if (per_sm < 1) per_sm = 1;
   long long grid = (long long)di.sms * per_sm;
   const long long cta_items = small ? (ka.items + KG_THREADS / 32 - 1) / (KG_THREADS / 32) : ka.items;
   if (grid > cta_items) grid = cta_items;
   void* args[] = {&ka};
-  const cudaError_t e = cudaLaunchKernel(cfg.func, dim3((unsigned)grid), dim3(KG_THREADS), args, 0, s);
+  const cudaError_t e = cudaLaunchKernel(cfg.func, dim3((unsigned)grid),
+                                         dim3(bulk ? KB_THREADS : KG_THREADS), args, smem, s);
   return e == cudaSuccess ? KMX_OK : KMX_ERR_CUDA;
 }
 
