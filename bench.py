@@ -554,6 +554,12 @@ def run_ours(args):
 # Secondary workloads (one JSON line each; the default run is the headline).
 # ---------------------------------------------------------------------------
 
+def _selected(args, tag):
+    """Whether the case with this tag runs (--cases; empty: every case)."""
+    want = [c for c in getattr(args, "cases", "").split(",") if c]
+    return not want or tag in want
+
+
 def _events_time(torch, fn, K, W):
     for _ in range(W):
         fn()
@@ -669,6 +675,8 @@ def run_grad(args):
 
     out = []
     for d, n, batch in ((6, 5, 1024), (3, 8, 4096)):
+        if not _selected(args, f"{d}-{n}"):
+            continue
         N = n ** d
         g = torch.Generator(device="cuda").manual_seed(SEED + d)
         A = torch.randn((batch, d, n, n), dtype=torch.float64, device="cuda", generator=g) / n ** 0.5
@@ -713,7 +721,8 @@ def run_grad(args):
         del res
     kmx.check_device_status()
     print(json.dumps({"metric": "fused forward+backward time / forward time, FP64 data, both in "
-                                "the default form (double-float), d=6 n=5 batch 1024",
+                                f"the default form (double-float), d={out[0]['d']} "
+                                f"n={out[0]['n']} batch {out[0]['batch']}",
                       "value": out[0]["ratio_split_fwd_bwd_vs_split_fwd"], "unit": "ratio",
                       "higher_is_better": False, "workload": "grad", "cases": out,
                       "data": "synthetic"}))
@@ -844,6 +853,8 @@ def run_kgemm(args):
     out = []
     for trans, dt in (("nn", torch.float64), ("nt", torch.float64), ("nn", torch.float32)):
         for n in (2, 3, 4, 5, 6):
+            if not _selected(args, f"{trans}-{'f64' if dt == torch.float64 else 'f32'}-{n}"):
+                continue
             big = n ** 5
             mm, nn, kk = (n, big, n) if trans == "nn" else (big, n, n)
             esz = 8 if dt == torch.float64 else 4
@@ -1104,6 +1115,9 @@ def main():
     ap.add_argument("--entries", type=int, default=ENTRIES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cases", default="",
+                    help="comma-separated case tags to run (grad: d-n, e.g. 3-8; kgemm: "
+                         "trans-dtype-n, e.g. nn-f32-4); default: every case")
     ap.add_argument("--workload",
                     choices=["xbatched", "mixed", "grad", "precision", "kgemm", "big", "rect",
                              "small"],
