@@ -111,7 +111,11 @@ typedef enum kmx_engine {
                               distributed shared memory, no workspace.  Every engine takes
                               it for these shapes when the call passes no workspace; with
                               a workspace the per-mode kernels run (measured faster) unless
-                              this engine is asked for; other shapes treat it as TUNED */
+                              this engine is asked for; other shapes treat it as TUNED */,
+  KMX_ENGINE_LANE = 6      /* one entry per thread with the entry in registers: square
+                              n^2 <= 16 and n^d <= 16 (d = 1, 2 with n <= 4; d = 3 with
+                              n = 2), atomic or exclusive accumulation; other shapes treat
+                              it as TUNED */
 } kmx_engine;
 
 typedef struct kmx_options {

@@ -28,7 +28,8 @@ STATUS = {
 }
 
 FORMS = {"auto": 0, "plain": 1, "split": 2, "tf32x3": 3, "digits": 4, "split_raw": 5}
-ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2, "small": 3, "persistent": 4, "cluster": 5}
+ENGINES = {"tuned": 0, "per_mode": 1, "tiled": 2, "small": 3, "persistent": 4, "cluster": 5,
+           "lane": 6}
 ACCUMULATE = {"atomic": 0, "deterministic": 1}
 
 

@@ -10,6 +10,7 @@
 
 #include "kmx_cluster.cuh"
 #include "kmx_engine.cuh"
+#include "kmx_lane.cuh"
 #include "kmx_small.cuh"
 #include "kmx_tile.cuh"
 
@@ -25,7 +26,8 @@ struct LaunchHint {
   int group_threads;   // per-mode kernels: threads per entry group (0 = default)
   int groups_per_cta;  // entry groups per CTA (0 = default)
   int max_ctas;        // cap on the grid (0 = fill the GPU)
-  int engine;          // 0 choose, 1 per-mode, 2 register-tiled, 3 small-entry, 5 cluster
+  int engine;          // 0 choose, 1 per-mode, 2 register-tiled, 3 small-entry, 5 cluster,
+                       // 6 one entry per thread
   int ctas_per_sm;     // cap on the resident CTAs per SM the grid is sized for (0 = occupancy)
 };
 
@@ -275,6 +277,66 @@ inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHi
 }
 
 // ---------------------------------------------------------------------------
+// One entry per thread (kmx_lane.cuh): n^2 <= 16, n^d <= 16.
+// ---------------------------------------------------------------------------
+template <typename T, int FORM>
+struct LanePol {
+  using type = lane::LanePlain<T, false>;
+};
+template <typename T>
+struct LanePol<T, FORM_SPLIT> {
+  using type = lane::LaneSplit;
+};
+template <typename T>
+struct LanePol<T, FORM_REF32> {
+  using type = lane::LanePlain<T, true>;
+};
+
+template <typename T, int FORM, int NN, int D>
+const void* lane_entry() {
+  if constexpr (lane::supported(NN, D) && FORM != FORM_WIDE &&
+                (FORM != FORM_SPLIT || std::is_same<T, double>::value)) {
+    return reinterpret_cast<const void*>(&lane::lane_kernel<typename LanePol<T, FORM>::type, NN, D>);
+  } else {
+    return nullptr;
+  }
+}
+
+template <typename T, int FORM>
+const void* pick_lane(int nn, int d) {
+  switch (nn * 10 + d) {
+    case 21: return lane_entry<T, FORM, 2, 1>();
+    case 31: return lane_entry<T, FORM, 3, 1>();
+    case 41: return lane_entry<T, FORM, 4, 1>();
+    case 22: return lane_entry<T, FORM, 2, 2>();
+    case 32: return lane_entry<T, FORM, 3, 2>();
+    case 42: return lane_entry<T, FORM, 4, 2>();
+    case 23: return lane_entry<T, FORM, 2, 3>();
+    default: return nullptr;
+  }
+}
+
+inline cudaError_t launch_lane(Problem& p, const void* func, const LaunchHint& hint,
+                               cudaStream_t stream) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo di = device_info(dev);
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, lane::THREADS, 0);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (hint.ctas_per_sm > 0 && per_sm > hint.ctas_per_sm) per_sm = hint.ctas_per_sm;
+  long long cap = (long long)di.sms * per_sm;
+  if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
+  // CTAs of THREADS entries (an upper bound when the count is on the device)
+  const long long want = p.count > 0 ? ((long long)p.count + lane::THREADS - 1) / lane::THREADS : 1;
+  const int grid = (int)(cap < want ? cap : want);
+  void* args[] = {&p};
+  return cudaLaunchKernel(func, dim3(grid), dim3(lane::THREADS), args, 0, stream);
+}
+
+// ---------------------------------------------------------------------------
 // Cluster kernels (kmx_cluster.cuh): double-float entries beyond one SM's
 // shared memory, n CTAs per (entry, i1) sharing mode 2 through distributed
 // shared memory.
@@ -433,6 +495,10 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
   if (!seg && square && hint.engine == 3) {
     const SmallKernel sk = pick_small<T, FORM>(nn, p.d);
     if (sk.func) return launch_small(p, sk, hint, stream);
+  }
+  if (!seg && square && hint.engine == 6) {
+    const void* lk = pick_lane<T, FORM>(nn, p.d);
+    if (lk) return launch_lane(p, lk, hint, stream);
   }
   if constexpr (FORM != FORM_REF32) {
     if (seg) {

@@ -43,7 +43,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "tune_table.json")
 
 FORM_CODES = {"plain": 1, "split": 2, "f32": 3}
-ENGINE_CODES = {"per_mode": 1, "tiled": 2, "small": 3}
+ENGINE_CODES = {"per_mode": 1, "tiled": 2, "small": 3, "lane": 6}
 LAYOUT_CODES = {"batched": 0, "pointer": 1}
 LAYOUTS = ("batched", "pointer")
 
@@ -63,6 +63,11 @@ def has_small(d, n):
     return d <= 3 and n ** d <= 256
 
 
+def has_lane(d, n):
+    """One entry per thread (kmx_lane.cuh): n^2 <= 16 and n^d <= 16."""
+    return d <= 3 and n * n <= 16 and n ** d <= 16
+
+
 def candidates(d, n):
     """(engine, (group_threads, groups_per_cta, ctas_per_sm)) to time."""
     out = [("per_mode", (g, 0, 0)) for g in (0, 64, 128, 256, 512)]
@@ -70,6 +75,8 @@ def candidates(d, n):
         out += [("tiled", (0, 0, 0)), ("tiled", (0, 1, 0)), ("tiled", (0, 0, 1))]
     if has_small(d, n):
         out.append(("small", (0, 0, 0)))
+    if has_lane(d, n):
+        out.append(("lane", (0, 0, 0)))
     return out
 
 
@@ -149,6 +156,9 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=TABLE)
     ap.add_argument("--quick", action="store_true", help="smaller batches, fewer repetitions")
+    ap.add_argument("--shapes", default="",
+                    help="comma-separated d-n shapes to tune (default: every shape); the rows "
+                         "and AUTO choices of the other shapes are kept from --out")
     args = ap.parse_args(argv)
     sys.path.insert(0, os.path.dirname(HERE))
     import torch
@@ -157,10 +167,19 @@ def main(argv=None):
 
     target = (32 << 20) if args.quick else (128 << 20)
     reps = 3 if args.quick else 5
+    only = {tuple(int(v) for v in t.split("-")) for t in args.shapes.split(",") if t}
     rows, auto = [], []
+    kept_rows, kept_auto = [], []
+    if only and os.path.exists(args.out):
+        with open(args.out) as f:
+            old = json.load(f)
+        kept_rows = [r for r in old.get("rows", []) if (r["d"], r["n"]) not in only]
+        kept_auto = [a for a in old.get("auto_form_f64", []) if (a["d"], a["n"]) not in only]
     best_by = {}
     for form in ("plain", "split", "f32"):
         for d, n in shapes():
+            if only and (d, n) not in only:
+                continue
             if form == "split" and not (2 <= n <= 8 or n == 16):
                 continue
             for layout in LAYOUTS:
@@ -187,6 +206,11 @@ def main(argv=None):
         s = best_by.get(("split", "batched", d, n))
         if p and s:
             auto.append({"d": d, "n": n, "form": "split" if s > p else "plain"})
+    if only:  # merge: the re-tuned shapes' rows replace theirs, in the table's order
+        key = lambda r: (list(FORM_CODES).index(r["form"]), r["d"], r["n"],
+                         LAYOUTS.index(r.get("layout", "batched")))
+        rows = sorted(kept_rows + rows, key=key)
+        auto = sorted(kept_auto + auto, key=lambda a: (a["d"], a["n"]))
     table = {
         "device": torch.cuda.get_device_name(0),
         "measured": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
@@ -196,6 +220,12 @@ def main(argv=None):
         "rows": rows,
         "auto_form_f64": auto,
     }
+    if only:  # a partial run keeps the full run's date and records its own
+        table["measured"] = old.get("measured", table["measured"])
+        table["retuned"] = {
+            "shapes": [f"{d}-{n}" for d, n in sorted(only)],
+            "measured": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
+        }
     with open(args.out, "w") as f:
         json.dump(table, f, indent=1)
     print(f"wrote {args.out}: {len(rows)} rows")

@@ -1,5 +1,7 @@
 """GPU parity of the small-entry kernels (engine KMX_ENGINE_SMALL: d <= 3 with
-n^d <= 256, many entries per CTA) against the oracle, through the C ABI.
+n^d <= 256, many entries per CTA) and of the one-entry-per-thread kernels
+(engine KMX_ENGINE_LANE: n^2 <= 16 and n^d <= 16) against the oracle, through
+the C ABI.
 
 Covers the contiguous batched layout (staged with 128-bit loads, and at an
 offset that breaks 16-byte alignment), the pointer layouts with overlapping Y
@@ -22,6 +24,15 @@ SHAPES = [(1, 2), (1, 3), (1, 4), (1, 8), (1, 16), (2, 2), (2, 3), (2, 4), (2, 7
           (2, 16), (3, 2), (3, 3), (3, 4), (3, 6)]
 
 
+ENGINES = ["small", "lane"]
+
+
+def engine_shape(engine, d, n):
+    """Skip a lane-engine case whose shape that kernel does not take."""
+    if engine == "lane" and not (d <= 3 and n * n <= 16 and n ** d <= 16):
+        pytest.skip("shape beyond the one-entry-per-thread kernel")
+
+
 @pytest.fixture(scope="module", autouse=True)
 def _need_gpu():
     if not torch.cuda.is_available():
@@ -38,9 +49,11 @@ def ulps(y, ref):
     return np.abs(np.asarray(y, dtype=np.float64).ravel() - ref32.astype(np.float64)) / sp
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("d,n", SHAPES)
 @pytest.mark.parametrize("form", ["plain", "split"])
-def test_small_batched_f64(kmx, oracle, d, n, form):
+def test_small_batched_f64(kmx, oracle, d, n, form, engine):
+    engine_shape(engine, d, n)
     rng = np.random.default_rng(50 + 10 * d + n)
     N = n ** d
     batch = 1237  # several chunks and a ragged tail
@@ -52,13 +65,15 @@ def test_small_batched_f64(kmx, oracle, d, n, form):
     for offset in (0, 1):  # offset 1: X no longer 16-byte aligned
         Xd = dev(np.concatenate([np.zeros(offset), X.ravel()]))[offset:]
         Yd = dev(Y0)
-        kmx.kronmult_batched(d, n, dev(A), Xd, Yd, None, batch, form=form, engine="small")
+        kmx.kronmult_batched(d, n, dev(A), Xd, Yd, None, batch, form=form, engine=engine)
         assert blockwise_rel_err(Yd.cpu().numpy() - Y0, Yref - Y0) <= 1e-13, offset
     assert kmx.check_device_status() == 0
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("d,n", SHAPES)
-def test_small_batched_f32(kmx, oracle, d, n):
+def test_small_batched_f32(kmx, oracle, d, n, engine):
+    engine_shape(engine, d, n)
     rng = np.random.default_rng(70 + 10 * d + n)
     N = n ** d
     batch = 999
@@ -68,20 +83,22 @@ def test_small_batched_f32(kmx, oracle, d, n):
     Yref = Y0.copy()
     oracle.batched(d, n, A, X.copy(), Yref, np.zeros_like(X), batch)
     Yd = dev(Y0)
-    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, engine="small")  # reference form
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, engine=engine)  # reference form
     u = ulps(Yd.cpu().numpy(), Yref)
     assert np.mean(u <= 1.0) >= 0.999 and u.max() <= 8.0, (float(np.mean(u <= 1)), float(u.max()))
     Yp = dev(Y0)
-    kmx.kronmult_batched(d, n, dev(A), dev(X), Yp, None, batch, form="plain", engine="small")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yp, None, batch, form="plain", engine=engine)
     assert ref_test_err(Yp.cpu().numpy(), Yref) <= 1e-5
     assert kmx.check_device_status() == 0
 
 
-@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 8), (3, 4)])
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 8), (3, 2), (3, 4)])
 @pytest.mark.parametrize("form", ["plain", "split"])
 @pytest.mark.parametrize("transpose", [False, True])
-def test_small_xbatched_overlap(kmx, oracle, d, n, form, transpose):
+def test_small_xbatched_overlap(kmx, oracle, d, n, form, transpose, engine):
     """Pointer layout, lda = n + 2, Y blocks shared by many entries (atomics)."""
+    engine_shape(engine, d, n)
     rng = np.random.default_rng(90 + d * n)
     N = n ** d
     pool, nx, ny, ne, lda = 16, 40, 13, 2000, n + 2
@@ -107,17 +124,25 @@ def test_small_xbatched_overlap(kmx, oracle, d, n, form, transpose):
     pX = kmx.pointer_array(Xd, x_idx * N)
     pY = kmx.pointer_array(Yd, y_idx * N)
     kmx.kronmult_xbatched(d, n, pA, lda, pX, pY, None, ne, form=form, transpose=transpose,
-                          engine="small")
+                          engine=engine)
     assert kmx.check_device_status() == 0
     assert blockwise_rel_err(Yd.cpu().numpy() - Y0, Yref - Y0) <= 1e-13
 
 
-@pytest.mark.parametrize("d,n", [(1, 8), (2, 4), (3, 3)])
-def test_small_split_special_entries(kmx, oracle, d, n):
-    """Double-float in the small kernel: entries with Inf/NaN (FP64 path,
-    IEEE propagation), an all-zero factor (exact zero), and cancelling entries
-    (rows summing to zero on X = 1 + 1e-2 Z: recomputed in FP64 by the guard,
-    counted) among ordinary ones."""
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("d,n", [(1, 3), (1, 8), (2, 2), (2, 4), (3, 2), (3, 3)])
+def test_small_split_special_entries(kmx, oracle, d, n, engine):
+    """Double-float in the small and lane kernels: entries with Inf/NaN (FP64
+    path, IEEE propagation), an all-zero factor (exact zero), and cancelling
+    entries (rows summing to zero on X = 1 + 1e-2 Z: recomputed in FP64 by the
+    guard, counted) among ordinary ones.  Held to 1e-13 per block for n >= 3
+    and blocks of 8 or more elements; n = 2 and smaller blocks to 5e-13: the
+    guard keeps entries down to rho_F = 1/4, where the double-float bound
+    c 2^-48 sqrt(N) / rho_F is widest relative to the block, and two-term dot
+    products do not average the rounding errors (measured: d=2 n=2 3.9e-13,
+    d=3 n=2 1.6e-13, d=1 n=3 1.06e-13; the automatic form runs plain FP64 for
+    all of these shapes)."""
+    engine_shape(engine, d, n)
     rng = np.random.default_rng(123 + d * n)
     N = n ** d
     batch = 700
@@ -134,7 +159,7 @@ def test_small_split_special_entries(kmx, oracle, d, n):
     Yx = oracle.kron_batched_extended(d, n, A, X).astype(np.float64)
     Yd = dev(Y0)
     kmx.read_redo_counters()
-    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", engine="small")
+    kmx.kronmult_batched(d, n, dev(A), dev(X), Yd, None, batch, form="split", engine=engine)
     guard, _ = kmx.read_redo_counters()
     assert kmx.check_device_status() == 0
     y = Yd.cpu().numpy()
@@ -143,5 +168,5 @@ def test_small_split_special_entries(kmx, oracle, d, n):
     assert np.array_equal(np.isinf(y[~fin]), np.isinf(Yx[~fin]))
     assert not y[5].any()
     ok = fin & (np.arange(batch) != 5)
-    assert blockwise_rel_err(y[ok], Yx[ok]) <= 1e-13
+    assert blockwise_rel_err(y[ok], Yx[ok]) <= (1e-13 if n >= 3 and N >= 8 else 5e-13)
     assert guard >= int(canc.sum())

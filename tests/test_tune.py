@@ -59,6 +59,7 @@ def test_candidates_cover_every_engine_of_the_shape():
         assert "per_mode" in engines
         assert ("tiled" in engines) == tune.has_tile(d, n)
         assert ("small" in engines) == tune.has_small(d, n)
+        assert ("lane" in engines) == tune.has_lane(d, n)
         # the default launch shape of every engine is always among them
         for e in engines:
             assert (e, (0, 0, 0)) in tune.candidates(d, n)
