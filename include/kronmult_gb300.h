@@ -64,7 +64,9 @@ typedef enum kmx_form {
                           whose result cancels (rho_F = ||KX|| sqrt(prod n_l) /
                           (prod ||A_l||_F ||X||) below 1/4) is recomputed in FP64, so the
                           form is as accurate as PLAIN wherever PLAIN holds 1e-13
-                          (kmx_read_redo_counters counts those entries) */
+                          (kmx_read_redo_counters counts those entries), except on the
+                          smallest blocks: n = 2 (and d = 1, n = 3) measured up to 4e-13
+                          per block; AUTO runs FP64 for those shapes */
   KMX_FORM_DIGITS = 4, /* FP64 data on the FP16 tensor cores: X and factors as 7 base-2^9
                           digits with one exponent per entry, exact digit products
                           (mma.sync), exact FP32 level sums, FP64 out.  Square n = 4
