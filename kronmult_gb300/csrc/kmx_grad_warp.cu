@@ -4,19 +4,18 @@
 // The fused kernels of kmx_grad.cu give each entry a CTA.  An entry of a few
 // hundred elements (d = 3, n = 8: 512) then keeps most of that CTA waiting at
 // block barriers between steps that each hold a few fibers per thread.  Here
-// a warp takes one entry at a time with its factors and d slots of its own
+// a warp takes one entry at a time with its factors and d + 1 slots of its own
 // region of shared memory, so every step is ordered by warp barriers alone:
 //   forward   X -> slot 0, F_{k+1} = A_k x_k F_k into slot k+1 (a lane owns
 //             whole mode-k fibers, two at a time), then Y += A_{d-1} x_{d-1}
-//             F_{d-1} (staged in slot 0, added with coalesced loads/stores);
-//   backward  B = G into slot 0; for k = d-1 .. 0: the Gram dA_k(a, b) += sum
+//             F_{d-1} (staged in slot d, added with coalesced loads/stores);
+//   backward  B = G into slot d; for k = d-1 .. 0: the Gram dA_k(a, b) += sum
 //             over the mode-k fibers of B[a] F_k[b] (lane (a, s) sums row a
-//             over every S-th fiber, then a shuffle tree adds the S partials
-//             of each row in a fixed order), then B = A_k^T x_k B in place; at
-//             k = 0 X is staged again into slot 1 (F_1 is dead by then) for
-//             the last Gram and dX += A_0^T x_0 B is staged in slot 0.
+//             over every S-th fiber; each output adds its S partials in lane
+//             order), then B = A_k^T x_k B in place; at k = 0, dX += A_0^T
+//             x_0 B, staged in slot 0 (X is dead once the last Gram has run).
 // Global memory is touched only by coalesced staging loads and the Y, dX and
-// dA updates.
+// dA updates.  The shapes are compile-time (n, d), so every stride folds.
 // FP64 data, in double-float (the split kernels' arithmetic and per-entry
 // power-of-two scales, as grad_split_kernel) or native FP64 (the plain form,
 // and in the split kernel the entries with Inf/NaN or an all-zero X, G or
