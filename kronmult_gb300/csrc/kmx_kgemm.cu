@@ -304,8 +304,9 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_stream_kernel(KgArgs<T> a) {
 //     double-length accumulation (exact products, two-sums, one rounding) as
 //     Acc<float>; the results leave by one cp.async.bulk store (beta == 0, or
 //     the blend) or one cp.reduce.async.bulk .add (beta == 1: element-wise
-//     atomic adds, the reference's atomicAdd epilogue), after which the
-//     stage's "empty" mbarrier releases it to the producer.
+//     atomic adds, the reference's atomicAdd epilogue); once that copy has
+//     read the stage (checked one item later, so the wait is off the item's
+//     path) the stage's "empty" mbarrier releases it to the producer.
 // Bulk copies cover each chunk from its first 16-byte boundary in whole 16-byte
 // units; the few elements before and after are read and written directly.
 // Items whose B or C is not contiguous (ldB != kk, ldC != mm) read and write
