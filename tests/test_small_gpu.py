@@ -170,3 +170,26 @@ def test_small_split_special_entries(kmx, oracle, d, n, engine):
     ok = fin & (np.arange(batch) != 5)
     assert blockwise_rel_err(y[ok], Yx[ok]) <= (1e-13 if n >= 3 and N >= 8 else 5e-13)
     assert guard >= int(canc.sum())
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("form", ["plain", "split"])
+@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (3, 2)])
+def test_small_null_entry_pointer_sets_device_status(kmx, d, n, form, engine):
+    """A NULL inside a device pointer array: the entry is skipped, the status
+    word reports it (no fault), and the other entries are computed."""
+    engine_shape(engine, d, n)
+    batch, N = 300, n ** d
+    A = torch.rand((batch, d, n, n), dtype=torch.float64, device="cuda")
+    X = torch.rand((batch, N), dtype=torch.float64, device="cuda")
+    Y = torch.zeros_like(X)
+    pX = kmx.pointer_array(X, [b * N for b in range(batch)])
+    pX[7] = 0
+    pY = kmx.pointer_array(Y, [b * N for b in range(batch)])
+    kmx.kronmult_pbatched(d, n, A, pX, pY, None, batch, form=form, engine=engine)
+    torch.cuda.synchronize()
+    with pytest.raises(kmx.KmxError):
+        kmx.check_device_status()
+    y = Y.cpu().numpy()
+    assert not y[7].any() and y[0].any() and y[batch - 1].any()
+    assert kmx.check_device_status() == 0  # cleared
