@@ -692,8 +692,10 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
   // the register tiles' several outputs per thread measure faster)
   const bool stream = sizeof(T) == 4 && !small && kk <= KG_SMALL_DIM &&
                       (trans_b ? (nn <= KG_SMALL_DIM) : (mm <= KG_SMALL_DIM));
-  // the nn streaming shapes take the bulk-copy kernel
-  const bool bulk = stream && !trans_b;
+  // the nn streaming shapes take the bulk-copy kernel, and so do nn matrices
+  // of at most 2048 outputs with 128 or more columns (one item per entry)
+  const bool bulk = sizeof(T) == 4 && !trans_b && kk <= KG_SMALL_DIM && mm <= KG_SMALL_DIM &&
+                    (stream || nn >= 128);
   KgConfig cfg = trans_b ? pick_kgemm<T, true>(mm, nn) : pick_kgemm<T, false>(mm, nn);
   size_t smem = 0;
   if (bulk) {
@@ -748,7 +750,8 @@ int kgemm_impl(bool trans_b, int mm, int nn, int kk, T alpha, const T* const* A,
                                                 smem);
   if (per_sm < 1) per_sm = 1;
   long long grid = (long long)di.sms * per_sm;
-  const long long cta_items = small ? (ka.items + KG_THREADS / 32 - 1) / (KG_THREADS / 32) : ka.items;
+  const long long cta_items =
+      (small && !bulk) ? (ka.items + KG_THREADS / 32 - 1) / (KG_THREADS / 32) : ka.items;
   if (grid > cta_items) grid = cta_items;
   void* args[] = {&ka};
   const cudaError_t e = cudaLaunchKernel(cfg.func, dim3((unsigned)grid),
