@@ -315,7 +315,8 @@ __global__ void __launch_bounds__(KG_THREADS) kgemm_stream_kernel(KgArgs<T> a) {
 // are compiled with mm = kk = n as constants: with run-time sizes the
 // guarded, fully unrolled loops cost 3.7x the instructions (ncu, n = 4).
 // Waits are bounded: one that runs out flags DF_WAIT_TIMEOUT, waits once more
-// for the stage's copies and leaves.
+// (with the same bound) for every bulk copy the producer may have issued into
+// the stages, and leaves.
 constexpr int KB_STAGES = 4;
 constexpr int KB_CONSUMERS = 256;
 constexpr int KB_THREADS = KB_CONSUMERS + 32;
@@ -543,6 +544,14 @@ __global__ void __launch_bounds__(KB_THREADS) kgemm_bulk_kernel(KgArgs<float> a)
     if (ct == 0 && !tile::mbar_wait(&full[s], par)) {
       atomicOr(a.status, DF_WAIT_TIMEOUT);
       tile::mbar_wait(&full[s], par);  // the stage's copies, once more
+      // The producer may already have issued items k+1 and k+2 (stages are
+      // released one item late, so items up to k-2 are free): wait for their
+      // copies too, under the same bound, so that no bulk copy is still
+      // writing shared memory when the CTA leaves.
+      for (int j = 1; j <= KB_STAGES - 2; ++j) {
+        if (it + (long long)j * gridDim.x >= a.items) break;
+        tile::mbar_wait(&full[(k + j) % KB_STAGES], (uint32_t)((k + j) / KB_STAGES) & 1u);
+      }
       sstop[0] = 1;
     }
     kb_consumer_sync();  // stage s has arrived (the leader saw its mbarrier)
