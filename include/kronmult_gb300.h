@@ -116,7 +116,8 @@ typedef enum kmx_engine {
                               this engine is asked for; other shapes treat it as TUNED */,
   KMX_ENGINE_LANE = 6      /* one entry per thread with the entry in registers: square
                               n^2 <= 16 and n^d <= 16 (d = 1, 2 with n <= 4; d = 3 with
-                              n = 2), atomic or exclusive accumulation; other shapes treat
+                              n = 2); and d = 2 with n = 5..8, one group of n lanes per
+                              entry; atomic or exclusive accumulation; other shapes treat
                               it as TUNED */
 } kmx_engine;
 

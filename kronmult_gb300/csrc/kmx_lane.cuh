@@ -1,6 +1,7 @@
 // kmx_lane.cuh -- one entry per thread, for square entries small enough to
 // live in a thread's registers: n^2 <= 16 per factor and n^d <= 16 elements
-// (d = 1, 2 with n <= 4; d = 3 with n = 2).
+// (d = 1, 2 with n <= 4; d = 3 with n = 2); and, in namespace group, d = 2
+// with n = 5..8, one group of n lanes per entry (described there).
 //
 // The small-entry kernels (kmx_small.cuh) spread an entry over one thread per
 // output element, so every per-entry quantity -- the scale exponents of X and
@@ -41,6 +42,7 @@ struct LanePlain {
   using S = T;  // storage type
   using V = T;
   static constexpr bool SPLIT = false;
+  static constexpr bool ROUNDED = RD;  // each dot product rounded once
   template <int NN>
   __device__ __forceinline__ static V dot(const V* a, const V* v) {
     return dot_n<T, RD, NN>(a, v);
@@ -233,6 +235,286 @@ __global__ void __launch_bounds__(THREADS) lane_kernel(const Problem p) {
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// d = 2 with n = 5..8: one group of n lanes per entry (32/n groups per warp).
+//
+// With the X block as the n x n matrix M(j1, j2) = X[j1*n + j2], lane r of
+// the group first holds column r of M (loads of consecutive elements across
+// the group) and forms column r of T = A1 M (mode 1, the reference's order);
+// T goes through the group's shared memory, and lane r then holds row r of T
+// and forms row r of Y = T A2^T (mode 2), which it adds to Y.  Every factor
+// row is read by all lanes of the group from shared memory, where each lane
+// stores the column it loaded.  Per-entry quantities (exponents, guard norms)
+// are reduced by n shuffles within the group; there is no block barrier, and
+// groups run independently (shuffles and syncs carry the group's mask).
+// Double-float dots run on packed FP32 pairs (two rows of the factor per
+// instruction, kmx_pack.cuh); entries the guard rejects or holding Inf/NaN
+// are evaluated in FP64 by the same group, mode by mode, before anything is
+// written.
+// ---------------------------------------------------------------------------
+namespace group {
+
+constexpr int THREADS = 128;
+constexpr int WARPS = THREADS / 32;
+
+__host__ __device__ constexpr bool supported(int NN, int D) {
+  return D == 2 && NN >= 5 && NN <= 8;
+}
+
+// Shared memory of one group, in 8-byte words: the two factors (row pairs
+// of (hi, lo) for the double-float form, else row-major T) and the n x (n+1)
+// transpose tile; rounded to 2 mod 16 words so that the groups of a warp start
+// on different banks.
+template <class Pol, int NN>
+struct Layout {
+  static constexpr int RP = (NN + 1) / 2;
+  static constexpr int FAC_WORDS =
+      Pol::SPLIT ? 2 * RP * NN : (int)((NN * NN * sizeof(typename Pol::S) + 7) / 8);
+  static constexpr int TILE_WORDS = (int)((NN * (NN + 1) * sizeof(typename Pol::S) + 7) / 8);
+  static constexpr int RAW = 2 * FAC_WORDS + TILE_WORDS;
+  static constexpr int WORDS = (RAW + 13) / 16 * 16 + 2;
+  static constexpr int GPW = 32 / NN;
+  static constexpr int CTA_WORDS = WARPS * GPW * WORDS;
+};
+
+// The group's maximum: n shuffles for n <= 6; one __reduce_max_sync for
+// n = 7, 8, where it needs fewer registers (the shuffles measured faster at
+// n = 5, 6, where the reduction raised the register count).
+template <int NN>
+__device__ __forceinline__ int gmax(int v, unsigned gm, int base) {
+  if constexpr (NN >= 7) {
+    return (int)__reduce_max_sync(gm, (unsigned)v);
+  } else {
+    int m = v;
+#pragma unroll
+    for (int k = 0; k < NN; ++k) m = max(m, __shfl_sync(gm, v, base + k));
+    return m;
+  }
+}
+// the group's sum, added in lane order (the same value in every lane)
+template <int NN>
+__device__ __forceinline__ float gsum(float v, unsigned gm, int base) {
+  float s = __shfl_sync(gm, v, base);
+#pragma unroll
+  for (int k = 1; k < NN; ++k) s = __fadd_rn(s, __shfl_sync(gm, v, base + k));
+  return s;
+}
+
+// Plain forms (and the FP64 evaluation of double-float entries): factors
+// read as rows from fr (row-major, shared memory) or, with fr == nullptr,
+// from global memory; the tile holds T.
+template <typename T, bool RD, int NN>
+__device__ __forceinline__ void plain_modes(const T* X, T* Y, const T* A0, const T* A1, int ld0,
+                                            int ld1, bool trans, bool excl, const T* f0,
+                                            const T* f1, T* tile, int r, unsigned gm) {
+  T v[NN], yo[NN];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) v[j] = X[j * NN + r];  // column r of M
+  if (excl) {  // row r of Y, loaded with X (no load latency at the end)
+#pragma unroll
+    for (int i = 0; i < NN; ++i) yo[i] = Y[r * NN + i];
+  }
+#pragma unroll
+  for (int i = 0; i < NN; ++i) {
+    T a[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) a[j] = f0 ? f0[i * NN + j] : fac(A0, ld0, trans, i, j);
+    tile[i * (NN + 1) + r] = dot_n<T, RD, NN>(a, v);
+  }
+  __syncwarp(gm);
+#pragma unroll
+  for (int j = 0; j < NN; ++j) v[j] = tile[r * (NN + 1) + j];  // row r of T
+#pragma unroll
+  for (int i = 0; i < NN; ++i) {
+    T a[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) a[j] = f1 ? f1[i * NN + j] : fac(A1, ld1, trans, i, j);
+    const T y = dot_n<T, RD, NN>(a, v);
+    if (excl) {
+      Y[r * NN + i] = yo[i] + y;
+    } else {
+      atomicAdd(Y + r * NN + i, y);
+    }
+  }
+}
+
+template <int NN>
+__device__ __noinline__ void fp64_group_entry(const double* X, double* Y, const double* A0,
+                                              const double* A1, int ld0, int ld1, bool trans,
+                                              bool excl, double* tile, int r, unsigned gm) {
+  __syncwarp(gm);  // every lane is done with the tile
+  plain_modes<double, false, NN>(X, Y, A0, A1, ld0, ld1, trans, excl, nullptr, nullptr, tile, r,
+                                 gm);
+}
+
+// Packed double-float dots of one mode: out[i] (i < NN) = sum_j A(i, j) v[j]
+// for the factor's row pairs fp (RowPair (rp, j) at fp[rp*NN + j]).
+template <int NN>
+__device__ __forceinline__ void split_mode(const pk2::RowPair* fp, const df (&v)[NN],
+                                           df (&out)[NN]) {
+  using pk2::u64;
+  u64 vh[NN], vl[NN], nvh[NN];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    vh[j] = pk2::bcast(v[j].hi);
+    vl[j] = pk2::bcast(v[j].lo);
+    nvh[j] = pk2::bcast(-v[j].hi);
+  }
+#pragma unroll
+  for (int rp = 0; rp < (NN + 1) / 2; ++rp) {
+    u64 oh, ol;
+    pk2::dot_pair<NN>(fp + rp * NN, vh, vl, nvh, oh, ol);
+    float h0, h1, l0, l1;
+    pk2::unpack(oh, h0, h1);
+    pk2::unpack(ol, l0, l1);
+    out[2 * rp] = df{h0, l0};
+    if (2 * rp + 1 < NN) out[2 * rp + 1] = df{h1, l1};
+  }
+}
+
+// Column r of factor a (a[i] = A(i, r), split with exponent e) into row
+// pairs: RowPair (rp, r) = ((A(2rp, r), A(2rp+1, r)) high parts, low parts).
+template <int NN>
+__device__ __forceinline__ float store_column(pk2::RowPair* fp, const double (&a)[NN], int e,
+                                              int r) {
+  float s2 = 0.f;
+#pragma unroll
+  for (int rp = 0; rp < (NN + 1) / 2; ++rp) {
+    const df x0 = split_scaled(a[2 * rp], e);
+    const df x1 = 2 * rp + 1 < NN ? split_scaled(a[2 * rp + 1], e) : df{0.f, 0.f};
+    s2 = __fmaf_rn(x0.hi, x0.hi, s2);
+    s2 = __fmaf_rn(x1.hi, x1.hi, s2);
+    pk2::RowPair q;
+    q.hi = pk2::pack(x0.hi, x1.hi);
+    q.lo = pk2::pack(x0.lo, x1.lo);
+    fp[rp * NN + r] = q;
+  }
+  return s2;
+}
+
+template <int NN>
+__device__ __forceinline__ void split_group_entry(const Problem& p, const double* X, double* Y,
+                                                  const double* A0, const double* A1, int ld0,
+                                                  int ld1, bool trans, bool excl, uint64_t* region,
+                                                  int r, unsigned gm, int base) {
+  using L = Layout<LaneSplit, NN>;
+  pk2::RowPair* f0 = reinterpret_cast<pk2::RowPair*>(region);
+  pk2::RowPair* f1 = f0 + L::RP * NN;
+  df* tile = reinterpret_cast<df*>(region + 2 * L::FAC_WORDS);
+  double xr[NN], c0[NN], c1[NN];
+  int ex = 0, e0 = 0, e1 = 0;
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    xr[j] = X[j * NN + r];
+    c0[j] = fac(A0, ld0, trans, j, r);
+    c1[j] = fac(A1, ld1, trans, j, r);
+    ex = max(ex, exp_field(xr[j]));
+    e0 = max(e0, exp_field(c0[j]));
+    e1 = max(e1, exp_field(c1[j]));
+  }
+  ex = gmax<NN>(ex, gm, base);
+  e0 = gmax<NN>(e0, gm, base);
+  e1 = gmax<NN>(e1, gm, base);
+  df v[NN];
+  float x2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    v[j] = split_scaled(xr[j], ex);
+    x2 = __fmaf_rn(v[j].hi, v[j].hi, x2);
+  }
+  float a2[2];
+  a2[0] = store_column<NN>(f0, c0, e0, r);
+  a2[1] = store_column<NN>(f1, c1, e1, r);
+  __syncwarp(gm);
+  df t[NN];
+  split_mode<NN>(f0, v, t);  // column r of T
+#pragma unroll
+  for (int i = 0; i < NN; ++i) tile[i * (NN + 1) + r] = t[i];
+  __syncwarp(gm);
+#pragma unroll
+  for (int j = 0; j < NN; ++j) v[j] = tile[r * (NN + 1) + j];  // row r of T
+  split_mode<NN>(f1, v, t);  // row r of Y
+  float out2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < NN; ++i) out2 = __fmaf_rn(t[i].hi, t[i].hi, out2);
+  x2 = gsum<NN>(x2, gm, base);
+  a2[0] = gsum<NN>(a2[0], gm, base);
+  a2[1] = gsum<NN>(a2[1], gm, base);
+  out2 = gsum<NN>(out2, gm, base);
+  const bool nonfinite = ex == 2047 || e0 == 2047 || e1 == 2047;
+  const bool zero = ex == 0 || e0 == 0 || e1 == 0;
+  if (nonfinite) {  // Inf/NaN propagate exactly as in FP64 (0 * Inf included)
+    fp64_group_entry<NN>(X, Y, A0, A1, ld0, ld1, trans, excl, reinterpret_cast<double*>(tile), r,
+                         gm);
+    return;
+  }
+  if (zero) return;  // an all-zero factor or X: kron(...) X is exactly zero
+  if (!p.guard_off && guard_fails(out2, x2, a2, 2, NN * NN)) {  // cancellation: FP64 instead
+    fp64_group_entry<NN>(X, Y, A0, A1, ld0, ld1, trans, excl, reinterpret_cast<double*>(tile), r,
+                         gm);
+    if (r == 0) count_redo(p.redo_ctr, 0);
+    return;
+  }
+  const int escale = (ex - 1023) + (e0 - 1023) + (e1 - 1023);
+#pragma unroll
+  for (int i = 0; i < NN; ++i) {
+    y_accumulate(Y + r * NN + i,
+                 f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale), excl);
+  }
+}
+
+// Group g of warp w takes entries (blockIdx.x*WARPS + w)*GPW + g, then every
+// (gridDim.x*WARPS*GPW)-th; lanes beyond the last whole group stay idle.
+// Double-float, n = 6 is held to 6 CTAs per SM (80 registers) and n = 7, 8
+// to 5 (96): measured 3-8 % faster than the compiler's choice (96 / 112 / 122
+// registers), with at most 28 bytes of spill.
+template <class Pol, int NN>
+__global__ void __launch_bounds__(THREADS, Pol::SPLIT ? (NN >= 7 ? 5 : (NN == 6 ? 6 : 0)) : 0)
+    group_kernel(const Problem p) {
+  using S = typename Pol::S;
+  using L = Layout<Pol, NN>;
+  __shared__ __align__(16) uint64_t sm[L::CTA_WORDS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane / NN, r = lane - g * NN;
+  if (g >= L::GPW) return;
+  const int base = g * NN;
+  const unsigned gm = ((1u << NN) - 1u) << base;
+  uint64_t* region = sm + (warp * L::GPW + g) * L::WORDS;
+  const long long count = launch_count(p);
+  const bool excl = p.y_exclusive != 0;
+  const bool trans = p.trans != 0;
+  const int ld0 = p.ld[0], ld1 = p.ld[1];
+  const long long stride = (long long)gridDim.x * WARPS * L::GPW;
+  for (long long e = ((long long)blockIdx.x * WARPS + warp) * L::GPW + g; e < count; e += stride) {
+    const long long ent = tile::entry_index(p, e);
+    const S* X = tile::x_ptr<S>(p, ent);
+    S* Y = tile::y_ptr<S>(p, ent);
+    const S* A0 = tile::a_ptr<S>(p, ent, 0);
+    const S* A1 = tile::a_ptr<S>(p, ent, 1);
+    if (X == nullptr || Y == nullptr || A0 == nullptr || A1 == nullptr) {
+      if (r == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    if constexpr (Pol::SPLIT) {
+      split_group_entry<NN>(p, X, Y, A0, A1, ld0, ld1, trans, excl, region, r, gm, base);
+    } else {
+      S* f0 = reinterpret_cast<S*>(region);
+      S* f1 = f0 + NN * NN;
+      S* tl = reinterpret_cast<S*>(region + 2 * L::FAC_WORDS);
+#pragma unroll
+      for (int i = 0; i < NN; ++i) {  // column r of each factor, stored row-major
+        f0[i * NN + r] = fac(A0, ld0, trans, i, r);
+        f1[i * NN + r] = fac(A1, ld1, trans, i, r);
+      }
+      __syncwarp(gm);
+      plain_modes<S, Pol::ROUNDED, NN>(X, Y, A0, A1, ld0, ld1, trans, excl, f0, f1, tl, r, gm);
+    }
+    __syncwarp(gm);  // the group's shared memory is free for the next entry
+  }
+}
+
+}  // namespace group
 
 }  // namespace lane
 }  // namespace kmx

@@ -277,7 +277,8 @@ inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHi
 }
 
 // ---------------------------------------------------------------------------
-// One entry per thread (kmx_lane.cuh): n^2 <= 16, n^d <= 16.
+// One entry per thread (kmx_lane.cuh): n^2 <= 16, n^d <= 16; and d = 2 with
+// n = 5..8, one group of n lanes per entry.
 // ---------------------------------------------------------------------------
 template <typename T, int FORM>
 struct LanePol {
@@ -292,18 +293,32 @@ struct LanePol<T, FORM_REF32> {
   using type = lane::LanePlain<T, true>;
 };
 
+struct LaneKernel {
+  const void* func = nullptr;
+  int threads = 0;
+  int per_cta = 0;  // entries one CTA takes at a time
+};
+
 template <typename T, int FORM, int NN, int D>
-const void* lane_entry() {
-  if constexpr (lane::supported(NN, D) && FORM != FORM_WIDE &&
-                (FORM != FORM_SPLIT || std::is_same<T, double>::value)) {
-    return reinterpret_cast<const void*>(&lane::lane_kernel<typename LanePol<T, FORM>::type, NN, D>);
-  } else {
-    return nullptr;
+LaneKernel lane_entry() {
+  LaneKernel k;
+  if constexpr (FORM != FORM_WIDE && (FORM != FORM_SPLIT || std::is_same<T, double>::value)) {
+    using Pol = typename LanePol<T, FORM>::type;
+    if constexpr (lane::supported(NN, D)) {
+      k.func = reinterpret_cast<const void*>(&lane::lane_kernel<Pol, NN, D>);
+      k.threads = lane::THREADS;
+      k.per_cta = lane::THREADS;
+    } else if constexpr (lane::group::supported(NN, D)) {
+      k.func = reinterpret_cast<const void*>(&lane::group::group_kernel<Pol, NN>);
+      k.threads = lane::group::THREADS;
+      k.per_cta = lane::group::WARPS * lane::group::Layout<Pol, NN>::GPW;
+    }
   }
+  return k;
 }
 
 template <typename T, int FORM>
-const void* pick_lane(int nn, int d) {
+LaneKernel pick_lane(int nn, int d) {
   switch (nn * 10 + d) {
     case 21: return lane_entry<T, FORM, 2, 1>();
     case 31: return lane_entry<T, FORM, 3, 1>();
@@ -311,29 +326,33 @@ const void* pick_lane(int nn, int d) {
     case 22: return lane_entry<T, FORM, 2, 2>();
     case 32: return lane_entry<T, FORM, 3, 2>();
     case 42: return lane_entry<T, FORM, 4, 2>();
+    case 52: return lane_entry<T, FORM, 5, 2>();
+    case 62: return lane_entry<T, FORM, 6, 2>();
+    case 72: return lane_entry<T, FORM, 7, 2>();
+    case 82: return lane_entry<T, FORM, 8, 2>();
     case 23: return lane_entry<T, FORM, 2, 3>();
-    default: return nullptr;
+    default: return LaneKernel();
   }
 }
 
-inline cudaError_t launch_lane(Problem& p, const void* func, const LaunchHint& hint,
+inline cudaError_t launch_lane(Problem& p, const LaneKernel& k, const LaunchHint& hint,
                                cudaStream_t stream) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
   const DeviceInfo di = device_info(dev);
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, lane::THREADS, 0);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.func, k.threads, 0);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (hint.ctas_per_sm > 0 && per_sm > hint.ctas_per_sm) per_sm = hint.ctas_per_sm;
   long long cap = (long long)di.sms * per_sm;
   if (hint.max_ctas > 0 && cap > hint.max_ctas) cap = hint.max_ctas;
-  // CTAs of THREADS entries (an upper bound when the count is on the device)
-  const long long want = p.count > 0 ? ((long long)p.count + lane::THREADS - 1) / lane::THREADS : 1;
+  // CTAs of per_cta entries (an upper bound when the count is on the device)
+  const long long want = p.count > 0 ? ((long long)p.count + k.per_cta - 1) / k.per_cta : 1;
   const int grid = (int)(cap < want ? cap : want);
   void* args[] = {&p};
-  return cudaLaunchKernel(func, dim3(grid), dim3(lane::THREADS), args, 0, stream);
+  return cudaLaunchKernel(k.func, dim3(grid), dim3(k.threads), args, 0, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -497,8 +516,8 @@ cudaError_t launch_forward(Problem& p, const LaunchHint& hint, cudaStream_t stre
     if (sk.func) return launch_small(p, sk, hint, stream);
   }
   if (!seg && square && hint.engine == 6) {
-    const void* lk = pick_lane<T, FORM>(nn, p.d);
-    if (lk) return launch_lane(p, lk, hint, stream);
+    const LaneKernel lk = pick_lane<T, FORM>(nn, p.d);
+    if (lk.func) return launch_lane(p, lk, hint, stream);
   }
   if constexpr (FORM != FORM_REF32) {
     if (seg) {

@@ -64,8 +64,9 @@ def has_small(d, n):
 
 
 def has_lane(d, n):
-    """One entry per thread (kmx_lane.cuh): n^2 <= 16 and n^d <= 16."""
-    return d <= 3 and n * n <= 16 and n ** d <= 16
+    """The lane engine (kmx_lane.cuh): one entry per thread for n^2 <= 16 and
+    n^d <= 16, one group of n lanes per entry for d = 2 with n = 5..8."""
+    return (d <= 3 and n * n <= 16 and n ** d <= 16) or (d == 2 and 5 <= n <= 8)
 
 
 def candidates(d, n):
@@ -220,12 +221,15 @@ def main(argv=None):
         "rows": rows,
         "auto_form_f64": auto,
     }
-    if only:  # a partial run keeps the full run's date and records its own
+    if only:  # a partial run keeps the full run's date and adds its own to the record
         table["measured"] = old.get("measured", table["measured"])
-        table["retuned"] = {
+        runs = old.get("retuned", [])
+        runs = [runs] if isinstance(runs, dict) else list(runs)
+        runs.append({
             "shapes": [f"{d}-{n}" for d, n in sorted(only)],
             "measured": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
-        }
+        })
+        table["retuned"] = runs
     with open(args.out, "w") as f:
         json.dump(table, f, indent=1)
     print(f"wrote {args.out}: {len(rows)} rows")
