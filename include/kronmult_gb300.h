@@ -66,7 +66,8 @@ typedef enum kmx_form {
                           form is as accurate as PLAIN wherever PLAIN holds 1e-13
                           (kmx_read_redo_counters counts those entries), except on the
                           smallest blocks: n = 2 (and d = 1, n = 3) measured up to 4e-13
-                          per block; AUTO runs FP64 for those shapes */
+                          per block; AUTO runs FP64 for every n = 2 shape and every
+                          block under 8 elements */
   KMX_FORM_DIGITS = 4, /* FP64 data on the FP16 tensor cores: X and factors as 7 base-2^9
                           digits with one exponent per entry, exact digit products
                           (mma.sync), exact FP32 level sums, FP64 out.  Square n = 4
@@ -116,9 +117,10 @@ typedef enum kmx_engine {
                               this engine is asked for; other shapes treat it as TUNED */,
   KMX_ENGINE_LANE = 6      /* one entry per thread with the entry in registers: square
                               n^2 <= 16 and n^d <= 16 (d = 1, 2 with n <= 4; d = 3 with
-                              n = 2); and d = 2 with n = 5..8, one group of n lanes per
-                              entry; atomic or exclusive accumulation; other shapes treat
-                              it as TUNED */
+                              n = 2); d = 2 with n = 5..8, one group of n lanes per
+                              entry; d >= 3 with n^(d-1) <= 32, one fiber per lane;
+                              atomic or exclusive accumulation; other shapes treat it
+                              as TUNED */
 } kmx_engine;
 
 typedef struct kmx_options {

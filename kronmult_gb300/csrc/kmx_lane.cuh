@@ -516,5 +516,287 @@ __global__ void __launch_bounds__(THREADS, Pol::SPLIT ? (NN >= 7 ? 5 : (NN == 6 
 
 }  // namespace group
 
+// ---------------------------------------------------------------------------
+// d >= 3 with n^(d-1) <= 32 (d = 3 with n = 3..5, d = 4 with n = 2, 3, d = 5, 6
+// with n = 2): one group of L = n^(d-1) lanes per entry, one fiber per lane
+// and mode.
+//
+// Mode k contracts index k (stride S_k = n^(d-1-k)); lane l's fiber in mode k
+// starts at b_k(l) = (l / S_k) n S_k + l % S_k, so mode 0 reads X with
+// consecutive lanes on consecutive elements (b_0(l) = l) and mode d-1 leaves
+// lane l the contiguous row Y[l n .. l n + n).  The intermediates live in the
+// group's shared memory with one pad word per n (row reads conflict-free);
+// each lane overwrites its own fiber in place (fibers of one mode partition
+// the block), with a group sync between modes.  Lane l < n^2 loads entry
+// (l % n, l / n) of every factor (a column-major sweep) and stores it,
+// split, into the factor's row layout.  Reductions: butterflies when L is a
+// power of two, else L shuffles (sums) and __reduce_max_sync (maxima); the
+// double-float dots, the guard and the FP64 path are those of the group kernel.
+// ---------------------------------------------------------------------------
+namespace fiber {
+
+constexpr int THREADS = 128;
+constexpr int WARPS = THREADS / 32;
+
+__host__ __device__ constexpr bool supported(int NN, int D) {
+  return D >= 3 && D <= 6 && NN >= 2 && ipow(NN, D - 1) <= 32 && !lane::supported(NN, D);
+}
+
+template <class Pol, int NN, int D>
+struct Layout {
+  static constexpr int L = ipow(NN, D - 1);
+  static constexpr int N = NN * L;
+  static constexpr int RP = (NN + 1) / 2;
+  static constexpr int FAC_WORDS =
+      Pol::SPLIT ? 2 * RP * NN : (int)((NN * NN * sizeof(typename Pol::S) + 7) / 8);
+  static constexpr int TILE_ELEMS = N + L;  // one pad per n
+  static constexpr int TILE_WORDS = (int)((TILE_ELEMS * sizeof(typename Pol::S) + 7) / 8);
+  static constexpr int RAW = D * FAC_WORDS + TILE_WORDS;
+  static constexpr int WORDS = (RAW + 13) / 16 * 16 + 2;
+  static constexpr int GPW = 32 / L;
+  static constexpr int CTA_WORDS = WARPS * GPW * WORDS;
+};
+
+template <int NN>
+__device__ __forceinline__ int pq(int q) {
+  return q + q / NN;
+}
+template <int NN, int D>
+__device__ __forceinline__ int fiber_base(int l, int k) {
+  const int S = ipow(NN, D - 1 - k);
+  return (l / S) * NN * S + l % S;
+}
+
+// Group-wide max and sum (every lane gets the same value).
+template <int L>
+__device__ __forceinline__ int fmax_g(int v, unsigned gm, int base) {
+  if constexpr ((L & (L - 1)) == 0) {
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) v = max(v, __shfl_xor_sync(gm, v, o));
+    return v;
+  } else {
+    return (int)__reduce_max_sync(gm, (unsigned)v);
+  }
+}
+template <int L>
+__device__ __forceinline__ float fsum_g(float v, unsigned gm, int base) {
+  if constexpr ((L & (L - 1)) == 0) {
+    // a butterfly: each level adds the same two partial sums in every lane
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) v = __fadd_rn(v, __shfl_xor_sync(gm, v, o));
+    return v;
+  } else {
+    return group::gsum<L>(v, gm, base);
+  }
+}
+
+// Plain forms and the FP64 path: factors as rows from f (shared memory) or,
+// with f == nullptr, from global memory; T the intermediate tile.
+template <typename T, bool RD, int NN, int D>
+__device__ __forceinline__ void plain_fibers(const T* X, T* Y, const T* const* A, const int* ld,
+                                             bool trans, bool excl, const T* f, T* tile, int l,
+                                             unsigned gm) {
+  constexpr int L = ipow(NN, D - 1), NN2 = NN * NN;
+  T v[NN], yo[NN];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) v[j] = X[l + j * L];
+  if (excl) {
+#pragma unroll
+    for (int i = 0; i < NN; ++i) yo[i] = Y[l * NN + i];
+  }
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const int S = ipow(NN, D - 1 - k);
+    const int b = fiber_base<NN, D>(l, k);
+    if (k > 0) {
+      __syncwarp(gm);  // mode k-1 is complete
+#pragma unroll
+      for (int j = 0; j < NN; ++j) v[j] = tile[pq<NN>(b + j * S)];
+    }
+    T out[NN];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) {
+      T a[NN];
+#pragma unroll
+      for (int j = 0; j < NN; ++j)
+        a[j] = f ? f[k * NN2 + i * NN + j] : fac(A[k], ld[k], trans, i, j);
+      out[i] = dot_n<T, RD, NN>(a, v);
+    }
+    if (k < D - 1) {
+#pragma unroll
+      for (int i = 0; i < NN; ++i) tile[pq<NN>(b + i * S)] = out[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < NN; ++i) {
+        if (excl) {
+          Y[l * NN + i] = yo[i] + out[i];
+        } else {
+          atomicAdd(Y + l * NN + i, out[i]);
+        }
+      }
+    }
+  }
+}
+
+template <int NN, int D>
+__device__ __noinline__ void fp64_fiber_entry(const double* X, double* Y, const double* const* A,
+                                              const int* ld, bool trans, bool excl, double* tile,
+                                              int l, unsigned gm) {
+  __syncwarp(gm);  // every lane is done with the tile
+  plain_fibers<double, false, NN, D>(X, Y, A, ld, trans, excl, nullptr, tile, l, gm);
+}
+
+template <int NN, int D>
+__device__ __forceinline__ void split_fiber_entry(const Problem& p, const double* X, double* Y,
+                                                  const double* const* A, const int* ld,
+                                                  bool trans, bool excl, uint64_t* region, int l,
+                                                  unsigned gm, int base) {
+  using Lay = Layout<LaneSplit, NN, D>;
+  constexpr int L = Lay::L, NN2 = NN * NN;
+  float* ff = reinterpret_cast<float*>(region);  // factor k: RowPairs at word k*FAC_WORDS
+  const pk2::RowPair* fp = reinterpret_cast<const pk2::RowPair*>(region);
+  df* tile = reinterpret_cast<df*>(region + D * Lay::FAC_WORDS);
+  double xr[NN], c[D];
+  int ex = 0, ea[D];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    xr[j] = X[l + j * L];
+    ex = max(ex, exp_field(xr[j]));
+  }
+  const int fi = l % NN, fj = l / NN;  // the factor entry this lane loads (l < n^2)
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    c[k] = l < NN2 ? fac(A[k], ld[k], trans, fi, fj) : 0.0;
+    ea[k] = exp_field(c[k]);
+  }
+  ex = fmax_g<L>(ex, gm, base);
+#pragma unroll
+  for (int k = 0; k < D; ++k) ea[k] = fmax_g<L>(ea[k], gm, base);
+  df v[NN], t[NN];
+  float x2 = 0.f, a2[D];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    v[j] = split_scaled(xr[j], ex);
+    x2 = __fmaf_rn(v[j].hi, v[j].hi, x2);
+  }
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const df a = split_scaled(c[k], ea[k]);
+    a2[k] = __fmul_rn(a.hi, a.hi);
+    if (l < NN2) {
+      // RowPair (fi/2, fj) of factor k: floats [hi(2rp), hi(2rp+1), lo(2rp), lo(2rp+1)]
+      float* q = ff + 2 * k * Lay::FAC_WORDS + 4 * ((fi >> 1) * NN + fj);
+      q[fi & 1] = a.hi;
+      q[2 + (fi & 1)] = a.lo;
+      if ((NN & 1) && fi == NN - 1) {  // the zero pad row of an odd n
+        q[1] = 0.f;
+        q[3] = 0.f;
+      }
+    }
+  }
+  __syncwarp(gm);
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const int S = ipow(NN, D - 1 - k);
+    const int b = fiber_base<NN, D>(l, k);
+    if (k > 0) {
+      __syncwarp(gm);  // mode k-1 is complete
+#pragma unroll
+      for (int j = 0; j < NN; ++j) v[j] = tile[pq<NN>(b + j * S)];
+    }
+    group::split_mode<NN>(fp + k * (Lay::FAC_WORDS / 2), v, t);
+    if (k < D - 1) {
+#pragma unroll
+      for (int i = 0; i < NN; ++i) tile[pq<NN>(b + i * S)] = t[i];
+    }
+  }
+  float out2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < NN; ++i) out2 = __fmaf_rn(t[i].hi, t[i].hi, out2);
+  x2 = fsum_g<L>(x2, gm, base);
+#pragma unroll
+  for (int k = 0; k < D; ++k) a2[k] = fsum_g<L>(a2[k], gm, base);
+  out2 = fsum_g<L>(out2, gm, base);
+  bool nonfinite = ex == 2047, zero = ex == 0;
+  int escale = ex - 1023;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    nonfinite = nonfinite || ea[k] == 2047;
+    zero = zero || ea[k] == 0;
+    escale += ea[k] - 1023;
+  }
+  if (nonfinite) {  // Inf/NaN propagate exactly as in FP64 (0 * Inf included)
+    fp64_fiber_entry<NN, D>(X, Y, A, ld, trans, excl, reinterpret_cast<double*>(tile), l, gm);
+    return;
+  }
+  if (zero) return;  // an all-zero factor or X: kron(...) X is exactly zero
+  if (!p.guard_off && guard_fails(out2, x2, a2, D, Lay::N)) {  // cancellation: FP64 instead
+    fp64_fiber_entry<NN, D>(X, Y, A, ld, trans, excl, reinterpret_cast<double*>(tile), l, gm);
+    if (l == 0) count_redo(p.redo_ctr, 0);
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < NN; ++i)
+    y_accumulate(Y + l * NN + i,
+                 f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale), excl);
+}
+
+// Group g of warp w takes entries (blockIdx.x*WARPS + w)*GPW + g, then every
+// (gridDim.x*WARPS*GPW)-th; lanes beyond the last whole group stay idle.
+template <class Pol, int NN, int D>
+__global__ void __launch_bounds__(THREADS) fiber_kernel(const Problem p) {
+  using S = typename Pol::S;
+  using Lay = Layout<Pol, NN, D>;
+  constexpr int L = Lay::L;
+  __shared__ __align__(16) uint64_t sm[Lay::CTA_WORDS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane / L, l = lane - g * L;
+  if (g >= Lay::GPW) return;
+  const int base = g * L;
+  const unsigned gm = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << base;
+  uint64_t* region = sm + (warp * Lay::GPW + g) * Lay::WORDS;
+  const long long count = launch_count(p);
+  const bool excl = p.y_exclusive != 0;
+  const bool trans = p.trans != 0;
+  int ld[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) ld[k] = p.ld[k];
+  const long long stride = (long long)gridDim.x * WARPS * Lay::GPW;
+  for (long long e = ((long long)blockIdx.x * WARPS + warp) * Lay::GPW + g; e < count;
+       e += stride) {
+    const long long ent = tile::entry_index(p, e);
+    const S* X = tile::x_ptr<S>(p, ent);
+    S* Y = tile::y_ptr<S>(p, ent);
+    const S* A[D];
+    bool null = X == nullptr || Y == nullptr;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      A[k] = tile::a_ptr<S>(p, ent, k);
+      null = null || A[k] == nullptr;
+    }
+    if (null) {
+      if (l == 0) atomicOr(p.status, DF_NULL_PTR);
+      continue;
+    }
+    if constexpr (Pol::SPLIT) {
+      split_fiber_entry<NN, D>(p, X, Y, A, ld, trans, excl, region, l, gm, base);
+    } else {
+      S* f = reinterpret_cast<S*>(region);  // factor k row-major at f + k*n^2
+      S* tl = reinterpret_cast<S*>(region + D * Lay::FAC_WORDS);
+      constexpr int NN2 = NN * NN;
+      if (l < NN2) {
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+          f[k * NN2 + (l % NN) * NN + l / NN] = fac(A[k], ld[k], trans, l % NN, l / NN);
+      }
+      __syncwarp(gm);
+      plain_fibers<S, Pol::ROUNDED, NN, D>(X, Y, A, ld, trans, excl, f, tl, l, gm);
+    }
+    __syncwarp(gm);  // the group's shared memory is free for the next entry
+  }
+}
+
+}  // namespace fiber
+
 }  // namespace lane
 }  // namespace kmx

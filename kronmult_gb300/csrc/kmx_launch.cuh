@@ -277,8 +277,9 @@ inline cudaError_t launch_small(Problem& p, const SmallKernel& k, const LaunchHi
 }
 
 // ---------------------------------------------------------------------------
-// One entry per thread (kmx_lane.cuh): n^2 <= 16, n^d <= 16; and d = 2 with
-// n = 5..8, one group of n lanes per entry.
+// The lane engine (kmx_lane.cuh): one entry per thread for n^2 <= 16,
+// n^d <= 16; one group of n lanes per entry for d = 2 with n = 5..8; one
+// group of n^(d-1) <= 32 lanes per entry (a fiber per lane) for d >= 3.
 // ---------------------------------------------------------------------------
 template <typename T, int FORM>
 struct LanePol {
@@ -312,6 +313,10 @@ LaneKernel lane_entry() {
       k.func = reinterpret_cast<const void*>(&lane::group::group_kernel<Pol, NN>);
       k.threads = lane::group::THREADS;
       k.per_cta = lane::group::WARPS * lane::group::Layout<Pol, NN>::GPW;
+    } else if constexpr (lane::fiber::supported(NN, D)) {
+      k.func = reinterpret_cast<const void*>(&lane::fiber::fiber_kernel<Pol, NN, D>);
+      k.threads = lane::fiber::THREADS;
+      k.per_cta = lane::fiber::WARPS * lane::fiber::Layout<Pol, NN, D>::GPW;
     }
   }
   return k;
@@ -331,6 +336,13 @@ LaneKernel pick_lane(int nn, int d) {
     case 72: return lane_entry<T, FORM, 7, 2>();
     case 82: return lane_entry<T, FORM, 8, 2>();
     case 23: return lane_entry<T, FORM, 2, 3>();
+    case 33: return lane_entry<T, FORM, 3, 3>();
+    case 43: return lane_entry<T, FORM, 4, 3>();
+    case 53: return lane_entry<T, FORM, 5, 3>();
+    case 24: return lane_entry<T, FORM, 2, 4>();
+    case 34: return lane_entry<T, FORM, 3, 4>();
+    case 25: return lane_entry<T, FORM, 2, 5>();
+    case 26: return lane_entry<T, FORM, 2, 6>();
     default: return LaneKernel();
   }
 }

@@ -65,8 +65,18 @@ def has_small(d, n):
 
 def has_lane(d, n):
     """The lane engine (kmx_lane.cuh): one entry per thread for n^2 <= 16 and
-    n^d <= 16, one group of n lanes per entry for d = 2 with n = 5..8."""
-    return (d <= 3 and n * n <= 16 and n ** d <= 16) or (d == 2 and 5 <= n <= 8)
+    n^d <= 16, one group of n lanes per entry for d = 2 with n = 5..8, one
+    group of n^(d-1) <= 32 lanes per entry for d >= 3."""
+    return ((d <= 3 and n * n <= 16 and n ** d <= 16) or (d == 2 and 5 <= n <= 8) or
+            (3 <= d <= 6 and n ** (d - 1) <= 32))
+
+
+def split_allowed(d, n):
+    """Whether the automatic FP64 form may be double-float: blocks of n >= 3
+    with 8 or more elements.  On smaller blocks (n = 2, and d = 1 with n = 3)
+    the guarded double-float form measured up to 4e-13 per block on cancelling
+    entries, above the 1e-13 that plain FP64 holds."""
+    return n >= 3 and n ** d >= 8
 
 
 def candidates(d, n):
@@ -206,7 +216,8 @@ def main(argv=None):
         p = best_by.get(("plain", "batched", d, n))
         s = best_by.get(("split", "batched", d, n))
         if p and s:
-            auto.append({"d": d, "n": n, "form": "split" if s > p else "plain"})
+            auto.append({"d": d, "n": n,
+                         "form": "split" if s > p and split_allowed(d, n) else "plain"})
     if only:  # merge: the re-tuned shapes' rows replace theirs, in the table's order
         key = lambda r: (list(FORM_CODES).index(r["form"]), r["d"], r["n"],
                          LAYOUTS.index(r.get("layout", "batched")))

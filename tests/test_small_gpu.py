@@ -1,8 +1,8 @@
 """GPU parity of the small-entry kernels (engine KMX_ENGINE_SMALL: d <= 3 with
 n^d <= 256, many entries per CTA) and of the lane kernels (engine
 KMX_ENGINE_LANE: one entry per thread for n^2 <= 16 and n^d <= 16, one group
-of n lanes per entry for d = 2 with n = 5..8) against the oracle, through the
-C ABI.
+of n lanes per entry for d = 2 with n = 5..8, one group of n^(d-1) <= 32
+lanes per entry for d >= 3) against the oracle, through the C ABI.
 
 Covers the contiguous batched layout (staged with 128-bit loads, and at an
 offset that breaks 16-byte alignment), the pointer layouts with overlapping Y
@@ -22,17 +22,21 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 SHAPES = [(1, 2), (1, 3), (1, 4), (1, 8), (1, 16), (2, 2), (2, 3), (2, 4), (2, 5), (2, 6),
-          (2, 7), (2, 8), (2, 16), (3, 2), (3, 3), (3, 4), (3, 6)]
+          (2, 7), (2, 8), (2, 16), (3, 2), (3, 3), (3, 4), (3, 5), (3, 6), (4, 2), (4, 3),
+          (5, 2), (6, 2)]
 
 
 ENGINES = ["small", "lane"]
 
 
 def engine_shape(engine, d, n):
-    """Skip a lane-engine case whose shape those kernels do not take."""
+    """Skip a case whose shape the engine's kernels do not take."""
     if engine == "lane" and not ((d <= 3 and n * n <= 16 and n ** d <= 16) or
-                                 (d == 2 and 5 <= n <= 8)):
+                                 (d == 2 and 5 <= n <= 8) or
+                                 (3 <= d <= 6 and n ** (d - 1) <= 32)):
         pytest.skip("shape beyond the lane kernels")
+    if engine == "small" and not (d <= 3 and n ** d <= 256):
+        pytest.skip("shape beyond the small-entry kernels")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -95,7 +99,8 @@ def test_small_batched_f32(kmx, oracle, d, n, engine):
 
 
 @pytest.mark.parametrize("engine", ENGINES)
-@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 5), (2, 8), (3, 2), (3, 4)])
+@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 5), (2, 8), (3, 2), (3, 4), (3, 5), (4, 3),
+                                 (6, 2)])
 @pytest.mark.parametrize("form", ["plain", "split"])
 @pytest.mark.parametrize("transpose", [False, True])
 def test_small_xbatched_overlap(kmx, oracle, d, n, form, transpose, engine):
@@ -132,7 +137,8 @@ def test_small_xbatched_overlap(kmx, oracle, d, n, form, transpose, engine):
 
 
 @pytest.mark.parametrize("engine", ENGINES)
-@pytest.mark.parametrize("d,n", [(1, 3), (1, 8), (2, 2), (2, 4), (2, 5), (2, 8), (3, 2), (3, 3)])
+@pytest.mark.parametrize("d,n", [(1, 3), (1, 8), (2, 2), (2, 4), (2, 5), (2, 8), (3, 2), (3, 3),
+                                 (3, 4), (4, 3), (5, 2)])
 def test_small_split_special_entries(kmx, oracle, d, n, engine):
     """Double-float in the small and lane kernels: entries with Inf/NaN (FP64
     path, IEEE propagation), an all-zero factor (exact zero), and cancelling
@@ -176,7 +182,7 @@ def test_small_split_special_entries(kmx, oracle, d, n, engine):
 
 @pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("form", ["plain", "split"])
-@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 6), (3, 2)])
+@pytest.mark.parametrize("d,n", [(1, 4), (2, 3), (2, 6), (3, 2), (3, 4)])
 def test_small_null_entry_pointer_sets_device_status(kmx, d, n, form, engine):
     """A NULL inside a device pointer array: the entry is skipped, the status
     word reports it (no fault), and the other entries are computed."""
