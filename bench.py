@@ -951,6 +951,8 @@ def run_small(args):
     for d, n in ((1, 2), (1, 4), (1, 8), (2, 4), (2, 8), (3, 4)):
         N = n ** d
         for form in ("plain", "split", "f32"):
+            if not _selected(args, f"{d}-{n}-{form}"):
+                continue
             dt = torch.float32 if form == "f32" else torch.float64
             esz = 4 if form == "f32" else 8
             batch = (256 << 20) // (N * esz)
@@ -972,6 +974,8 @@ def run_small(args):
             out.append(row)
             del A, X, Y
     kmx.check_device_status()
+    if not out:
+        raise SystemExit("--cases selected no small-entry case (tags: d-n-form)")
     print(json.dumps({"metric": "HBM fraction of small entries (batched, tuned engine)",
                       "value": out[0]["hbm_frac"], "unit": "fraction of measured HBM",
                       "workload": "small", "hbm_peak_gbs": peaks["hbm_gbs"],
@@ -1117,7 +1121,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cases", default="",
                     help="comma-separated case tags to run (grad: d-n, e.g. 3-8; kgemm: "
-                         "trans-dtype-n, e.g. nn-f32-4); default: every case")
+                         "trans-dtype-n, e.g. nn-f32-4; small: d-n-form, e.g. 2-8-split); "
+                         "default: every case")
     ap.add_argument("--workload",
                     choices=["xbatched", "mixed", "grad", "precision", "kgemm", "big", "rect",
                              "small"],

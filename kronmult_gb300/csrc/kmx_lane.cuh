@@ -1,7 +1,8 @@
 // kmx_lane.cuh -- one entry per thread, for square entries small enough to
 // live in a thread's registers: n^2 <= 16 per factor and n^d <= 16 elements
-// (d = 1, 2 with n <= 4; d = 3 with n = 2); and, in namespace group, d = 2
-// with n = 5..8, one group of n lanes per entry (described there).
+// (d = 1, 2 with n <= 4; d = 3 with n = 2); and, in namespaces group and
+// fiber, d = 2 with n = 5..8 (one group of n lanes per entry) and d >= 3 with
+// n^(d-1) <= 32 (one fiber per lane), described there.
 //
 // The small-entry kernels (kmx_small.cuh) spread an entry over one thread per
 // output element, so every per-entry quantity -- the scale exponents of X and
@@ -457,11 +458,14 @@ __device__ __forceinline__ void split_group_entry(const Problem& p, const double
     return;
   }
   const int escale = (ex - 1023) + (e0 - 1023) + (e1 - 1023);
+  // Y by atomic adds even where blocks are exclusive: the add runs in L2, off
+  // this kernel's busiest pipe (FP64: the widening adds and the split's
+  // int -> float conversions), and with one writer per block it rounds once,
+  // exactly as a read-modify-write would
 #pragma unroll
-  for (int i = 0; i < NN; ++i) {
-    y_accumulate(Y + r * NN + i,
-                 f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale), excl);
-  }
+  for (int i = 0; i < NN; ++i)
+    atomicAdd(Y + r * NN + i,
+              f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale));
 }
 
 // Group g of warp w takes entries (blockIdx.x*WARPS + w)*GPW + g, then every
@@ -735,10 +739,11 @@ __device__ __forceinline__ void split_fiber_entry(const Problem& p, const double
     if (l == 0) count_redo(p.redo_ctr, 0);
     return;
   }
+  // Y by atomic adds even where blocks are exclusive (as in the group kernel)
 #pragma unroll
   for (int i = 0; i < NN; ++i)
-    y_accumulate(Y + l * NN + i,
-                 f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale), excl);
+    atomicAdd(Y + l * NN + i,
+              f32_to_f64_scaled(t[i].hi, escale) + f32_to_f64_scaled(t[i].lo, escale));
 }
 
 // Group g of warp w takes entries (blockIdx.x*WARPS + w)*GPW + g, then every
