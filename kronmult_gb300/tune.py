@@ -163,6 +163,43 @@ def time_one(kmx, torch, d, n, form, engine, target_bytes, reps, layout="batched
     return Case(kmx, torch, d, n, form, layout, target_bytes).gflops(engine, launch, reps)
 
 
+def auto_forms(best_by):
+    """The automatic FP64 form per shape: the faster of plain and double-float
+    on the batched layout (best_by[(form, layout, d, n)] = GFLOP/s), plain
+    where split_allowed says no."""
+    auto = []
+    for d, n in shapes():
+        p = best_by.get(("plain", "batched", d, n))
+        s = best_by.get(("split", "batched", d, n))
+        if p and s:
+            auto.append({"d": d, "n": n,
+                         "form": "split" if s > p and split_allowed(d, n) else "plain"})
+    return auto
+
+
+def build_table(rows, auto, device, method, now, only=frozenset(), old=None):
+    """The table a run writes.  A partial run (only: the re-tuned (d, n)
+    shapes) keeps the other shapes' rows and automatic forms from the old
+    table, sorted in the table's order, keeps the full run's date and appends
+    its own shapes and date to the "retuned" record."""
+    table = {"device": device, "measured": now, "method": method, "rows": rows,
+             "auto_form_f64": auto}
+    if only:
+        old = old or {}
+        kept_rows = [r for r in old.get("rows", []) if (r["d"], r["n"]) not in only]
+        kept_auto = [a for a in old.get("auto_form_f64", []) if (a["d"], a["n"]) not in only]
+        key = lambda r: (list(FORM_CODES).index(r["form"]), r["d"], r["n"],
+                         LAYOUTS.index(r.get("layout", "batched")))
+        table["rows"] = sorted(kept_rows + rows, key=key)
+        table["auto_form_f64"] = sorted(kept_auto + auto, key=lambda a: (a["d"], a["n"]))
+        table["measured"] = old.get("measured", now)
+        runs = old.get("retuned", [])
+        runs = [runs] if isinstance(runs, dict) else list(runs)
+        runs.append({"shapes": [f"{d}-{n}" for d, n in sorted(only)], "measured": now})
+        table["retuned"] = runs
+    return table
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=TABLE)
@@ -179,14 +216,11 @@ def main(argv=None):
     target = (32 << 20) if args.quick else (128 << 20)
     reps = 3 if args.quick else 5
     only = {tuple(int(v) for v in t.split("-")) for t in args.shapes.split(",") if t}
-    rows, auto = [], []
-    kept_rows, kept_auto = [], []
+    old = None
     if only and os.path.exists(args.out):
         with open(args.out) as f:
             old = json.load(f)
-        kept_rows = [r for r in old.get("rows", []) if (r["d"], r["n"]) not in only]
-        kept_auto = [a for a in old.get("auto_form_f64", []) if (a["d"], a["n"]) not in only]
-    best_by = {}
+    rows, best_by = [], {}
     for form in ("plain", "split", "f32"):
         for d, n in shapes():
             if only and (d, n) not in only:
@@ -212,38 +246,15 @@ def main(argv=None):
                              "candidates": {label(*k): round(v, 1) for k, v in res.items()}})
                 best_by[(form, layout, d, n)] = g
                 print(form, layout, d, n, label(engine, launch), round(g, 1), flush=True)
-    for d, n in shapes():
-        p = best_by.get(("plain", "batched", d, n))
-        s = best_by.get(("split", "batched", d, n))
-        if p and s:
-            auto.append({"d": d, "n": n,
-                         "form": "split" if s > p and split_allowed(d, n) else "plain"})
-    if only:  # merge: the re-tuned shapes' rows replace theirs, in the table's order
-        key = lambda r: (list(FORM_CODES).index(r["form"]), r["d"], r["n"],
-                         LAYOUTS.index(r.get("layout", "batched")))
-        rows = sorted(kept_rows + rows, key=key)
-        auto = sorted(kept_auto + auto, key=lambda a: (a["d"], a["n"]))
-    table = {
-        "device": torch.cuda.get_device_name(0),
-        "measured": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
-        "method": (f"batched and pointer (xbatched, 8 entries per Y block) layouts, "
-                   f"~{target >> 20} MiB of X per call, CUDA events, {reps} calls after 2; "
-                   "best engine and launch shape"),
-        "rows": rows,
-        "auto_form_f64": auto,
-    }
-    if only:  # a partial run keeps the full run's date and adds its own to the record
-        table["measured"] = old.get("measured", table["measured"])
-        runs = old.get("retuned", [])
-        runs = [runs] if isinstance(runs, dict) else list(runs)
-        runs.append({
-            "shapes": [f"{d}-{n}" for d, n in sorted(only)],
-            "measured": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
-        })
-        table["retuned"] = runs
+    method = (f"batched and pointer (xbatched, 8 entries per Y block) layouts, "
+              f"~{target >> 20} MiB of X per call, CUDA events, {reps} calls after 2; "
+              "best engine and launch shape")
+    now = datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds")
+    table = build_table(rows, auto_forms(best_by), torch.cuda.get_device_name(0), method, now,
+                        only, old)
     with open(args.out, "w") as f:
         json.dump(table, f, indent=1)
-    print(f"wrote {args.out}: {len(rows)} rows")
+    print(f"wrote {args.out}: {len(table['rows'])} rows ({len(rows)} measured)")
 
 
 def header_from_table(path: str = TABLE) -> str:

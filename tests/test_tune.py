@@ -92,3 +92,51 @@ def test_header_accepts_rows_without_layout(tmp_path):
                              "auto_form_f64": []}))
     text = tune.header_from_table(str(p))
     assert "{2, 0, 6, 4, 2, 0, 0, 0}" in text
+
+
+def _row(form, layout, d, n, g):
+    return {"form": form, "layout": layout, "d": d, "n": n, "engine": "per_mode",
+            "group_threads": 0, "groups_per_cta": 0, "ctas_per_sm": 0, "gflops": g,
+            "candidates": {"per_mode": g}}
+
+
+def test_partial_run_replaces_its_shapes_and_appends_the_record():
+    old = {"measured": "T0", "rows": [_row("f32", "batched", 2, 3, 1.0),
+                                      _row("plain", "pointer", 1, 2, 2.0),
+                                      _row("plain", "batched", 2, 3, 3.0),
+                                      _row("plain", "batched", 1, 2, 4.0)],
+           "auto_form_f64": [{"d": 2, "n": 3, "form": "split"}, {"d": 1, "n": 2, "form": "plain"}],
+           "retuned": {"shapes": ["1-2"], "measured": "T1"}}  # a single record, older format
+    new = [_row("plain", "batched", 2, 3, 9.0)]
+    t = tune.build_table(new, [{"d": 2, "n": 3, "form": "plain"}], "dev", "m", "T2",
+                         {(2, 3)}, old)
+    got = [(r["form"], r["layout"], r["d"], r["n"], r["gflops"]) for r in t["rows"]]
+    assert got == [("plain", "batched", 1, 2, 4.0), ("plain", "pointer", 1, 2, 2.0),
+                   ("plain", "batched", 2, 3, 9.0)]  # the old (2, 3) rows are gone
+    assert t["auto_form_f64"] == [{"d": 1, "n": 2, "form": "plain"},
+                                  {"d": 2, "n": 3, "form": "plain"}]
+    assert t["measured"] == "T0"  # the full run's date
+    assert t["retuned"] == [{"shapes": ["1-2"], "measured": "T1"},
+                            {"shapes": ["2-3"], "measured": "T2"}]
+    full = tune.build_table(new, [], "dev", "m", "T3")
+    assert full["measured"] == "T3" and "retuned" not in full and full["rows"] == new
+    # a partial run without an old table starts an empty one
+    assert tune.build_table(new, [], "dev", "m", "T4", {(2, 3)})["retuned"][0]["measured"] == "T4"
+
+
+def test_auto_forms_keep_plain_where_double_float_misses_the_bound():
+    best = {("plain", "batched", 6, 2): 1.0, ("split", "batched", 6, 2): 2.0,
+            ("plain", "batched", 3, 4): 1.0, ("split", "batched", 3, 4): 2.0,
+            ("plain", "batched", 2, 8): 3.0, ("split", "batched", 2, 8): 2.0}
+    forms = {(a["d"], a["n"]): a["form"] for a in tune.auto_forms(best)}
+    assert forms == {(6, 2): "plain", (3, 4): "split", (2, 8): "plain"}
+
+
+def test_committed_retune_records_name_tuned_shapes():
+    t = _table()
+    runs = t.get("retuned", [])
+    assert isinstance(runs, list)
+    valid = {f"{d}-{n}" for d, n in tune.shapes()}
+    for run in runs:
+        assert run["shapes"] and set(run["shapes"]) <= valid, run
+        assert run["measured"] >= t["measured"], run
