@@ -140,3 +140,15 @@ def test_committed_retune_records_name_tuned_shapes():
     for run in runs:
         assert run["shapes"] and set(run["shapes"]) <= valid, run
         assert run["measured"] >= t["measured"], run
+
+
+def test_lane_shapes_match_the_launcher():
+    """tune.has_lane names exactly the shapes kmx_launch.cuh's pick_lane
+    dispatches (a mismatch would time another engine under the lane label)."""
+    src = open(os.path.join(ROOT, "kronmult_gb300", "csrc", "kmx_launch.cuh")).read()
+    body = src[src.index("LaneKernel pick_lane("):]
+    body = body[:body.index("default:")]
+    cases = {(int(d), int(n)) for n, d in
+             re.findall(r"case \d+: return lane_entry<T, FORM, (\d+), (\d+)>", body)}
+    assert cases, "pick_lane switch not found"
+    assert cases == {(d, n) for d, n in tune.shapes() if tune.has_lane(d, n)}
